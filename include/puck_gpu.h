@@ -1,0 +1,132 @@
+/*
+ * puck_gpu.h -- C ABI of the GB300 chart-parsing library (libpuck_gb300.so).
+ *
+ * This is the drop-in boundary for the hot path of dlwh/puck: the Scala host
+ * binds these symbols (Panama FFM or JNI) in place of JavaCL + the generated
+ * OpenCL kernels.  Each entry point names the reference interface it replaces
+ * (paths relative to the dlwh/puck project).
+ *
+ * Conventions: plain pointers and sizes, no ownership transfer unless stated.
+ * Sentences are passed as word ids (see puck_grammar_word_id) with CSR
+ * offsets: sentence i is word_ids[offsets[i] .. offsets[i+1]).
+ * Calls on one puck_parser are not thread-safe (the reference's public
+ * methods are `synchronized`, CLParser.scala:50-63); distinct parsers may be
+ * used from distinct threads.  No call aborts the process or traps the GPU;
+ * failures come back as puck_status codes with a message from
+ * puck_last_error.
+ */
+#ifndef PUCK_GPU_H
+#define PUCK_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum puck_status {
+  PUCK_OK = 0,
+  PUCK_ERR_OOM = 1,            /* device or host allocation failed */
+  PUCK_ERR_BAD_GRAMMAR = 2,    /* unreadable or inconsistent grammar.grz */
+  PUCK_ERR_SENT_TOO_LONG = 3,  /* sentence longer than the parser's max length */
+  PUCK_ERR_OOV = 4,            /* word id outside the grammar's vocabulary */
+  PUCK_ERR_DEVICE_TIMEOUT = 5, /* a bounded device wait gave up */
+  PUCK_ERR_INVALID_ARG = 6,
+  PUCK_ERR_CUDA = 7,           /* a CUDA runtime call failed */
+  PUCK_ERR_INTERNAL = 8,
+  PUCK_ERR_EMPTY = 9           /* empty sentence */
+} puck_status;
+
+typedef enum puck_decode {
+  PUCK_DECODE_AUTO = 0,    /* Viterbi tree for a Viterbi fine level, MBR otherwise (CLParser.scala:151-164) */
+  PUCK_DECODE_VITERBI = 1,
+  PUCK_DECODE_MBR = 2
+} puck_decode;
+
+typedef struct puck_grammar puck_grammar;
+typedef struct puck_parser puck_parser;
+
+/* Options of `new CLParser(data, maxAllocSize, profile)` (CLParser.scala:46-48)
+ * plus the RunParser/CLParser flags that shape a parse (RunParser.scala:34-43). */
+typedef struct puck_options {
+  int64_t mem_bytes;          /* device bytes the parser may use (--mem); <= 0: 80% of free memory */
+  int32_t device;             /* CUDA device ordinal */
+  int32_t profile;            /* non-zero: per-pass CUDA-event timings in puck_parser_stats */
+  int32_t decode;             /* puck_decode */
+  int32_t max_length;         /* longest sentence accepted (0: 100) */
+  int32_t max_batch_sentences;/* cap on sentences per batch (0: no cap beyond memory) */
+  float prune_threshold;      /* coarse-pass log max-marginal threshold (reference: -9, CLParser.scala:226) */
+  int32_t use_graphs;         /* non-zero: capture each batch's pass sequence in a CUDA graph */
+} puck_options;
+
+/* One node of a preorder tree (the reference's tree_t, CLViterbi.scala:378):
+ * top = nonterminal of the unary layer or -1 (no unary layer), bot = the
+ * child symbol (terminal index when width == 1, else nonterminal index),
+ * width = span length, score = the backtrace score.  A sentence of length n
+ * has 2n-1 nodes; the left child of node p is p+1 and the right child is
+ * p + 2*width(left).  MBR trees use the same layout with coarse symbol ids. */
+typedef struct puck_tree_node {
+  int32_t top;
+  int32_t bot;
+  int32_t width;
+  float score;
+} puck_tree_node;
+
+typedef struct puck_stats {
+  double ms_total, ms_inside, ms_outside, ms_masks, ms_decode, ms_h2d, ms_d2h;
+  int64_t cells, cells_pruned, batches, kernel_launches;
+  int64_t binary_work;        /* (rule, split) applications executed in the last call */
+} puck_stats;
+
+void puck_default_options(puck_options* opts);
+
+/* --- grammar (CLParserData.readSequence, CLParser.scala:1302-1305) ------ */
+puck_grammar* puck_grammar_load(const char* grz_path, puck_status* status);
+void puck_grammar_free(puck_grammar* g);
+int32_t puck_grammar_num_levels(const puck_grammar* g);
+/* Per-level sizes: out[0..7] = semiring(0 viterbi,1 real,2 logsum), n_nt,
+ * n_t, cell_size, mask_size, n_coarse, root, n_words. */
+puck_status puck_grammar_level_info(const puck_grammar* g, int32_t level, int32_t out[8]);
+/* Word string -> id in the vocabulary of the fine level; -1 if unknown. */
+int32_t puck_grammar_word_id(const puck_grammar* g, const char* word);
+
+/* --- parser (new CLParser / release, CLParser.scala:46-89) -------------- */
+puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts, puck_status* status);
+void puck_parser_destroy(puck_parser* p);
+
+/* CLParser.parse (CLParser.scala:50-53): coarse passes build pruning masks,
+ * the last level decodes.  nodes_out holds sum(2*len_i - 1) nodes; node
+ * block of sentence i starts at sum_{j<i}(2*len_j - 1).  sent_status (nsent
+ * entries, may be NULL) gets a per-sentence puck_status; a sentence that
+ * fails leaves its nodes zeroed (the reference prints "(())" for it). */
+puck_status puck_parse(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                       puck_tree_node* nodes_out, int32_t* sent_status);
+
+/* CLParser.partitions (CLParser.scala:55-58,189-206): log partition (Viterbi:
+ * best score) of each sentence under the last level, with the cascade's masks. */
+puck_status puck_partitions(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                            float* log_z, int32_t* sent_status);
+
+/* CLParser.insideOutside (CLParser.scala:60-63,171-182): full inside and
+ * outside passes of every level (results stay on the device). */
+puck_status puck_inside_outside(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent);
+
+/* Copies of the last call's device state, for tests and tools.  Valid only
+ * when the call ran as a single batch.  which: 0 inside, 1 outside chart
+ * (num_cells * cell_size floats), 2 masks produced by `level` for the next
+ * level (num_cells * mask_size int32), 3 inside scales, 4 outside scales
+ * (num_cells floats), 5 per-cell MBR {score, symbol} pairs (num_cells * 2). */
+puck_status puck_debug_copy(puck_parser* p, int32_t level, int32_t which, void* host_out, size_t bytes);
+int64_t puck_debug_num_cells(const puck_parser* p);
+
+puck_status puck_parser_stats(const puck_parser* p, puck_stats* out);
+
+/* Last error message of the calling thread; returns the full length. */
+size_t puck_last_error(char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PUCK_GPU_H */

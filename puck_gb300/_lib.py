@@ -1,0 +1,103 @@
+"""ctypes binding of libpuck_gb300.so (the C ABI declared in include/puck_gpu.h).
+
+The library is built in-tree (``puck_gb300/_build``).  There is no CPU
+fallback: if the shared object cannot be built or loaded, every entry point
+raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+STATUS = {0: "OK", 1: "OOM", 2: "BAD_GRAMMAR", 3: "SENT_TOO_LONG", 4: "OOV", 5: "DEVICE_TIMEOUT",
+          6: "INVALID_ARG", 7: "CUDA", 8: "INTERNAL", 9: "EMPTY"}
+
+
+class PuckError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("mem_bytes", ctypes.c_int64), ("device", ctypes.c_int32), ("profile", ctypes.c_int32),
+                ("decode", ctypes.c_int32), ("max_length", ctypes.c_int32),
+                ("max_batch_sentences", ctypes.c_int32), ("prune_threshold", ctypes.c_float),
+                ("use_graphs", ctypes.c_int32)]
+
+
+class TreeNode(ctypes.Structure):
+    _fields_ = [("top", ctypes.c_int32), ("bot", ctypes.c_int32), ("width", ctypes.c_int32),
+                ("score", ctypes.c_float)]
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("ms_total", ctypes.c_double), ("ms_inside", ctypes.c_double), ("ms_outside", ctypes.c_double),
+                ("ms_masks", ctypes.c_double), ("ms_decode", ctypes.c_double), ("ms_h2d", ctypes.c_double),
+                ("ms_d2h", ctypes.c_double), ("cells", ctypes.c_int64), ("cells_pruned", ctypes.c_int64),
+                ("batches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("binary_work", ctypes.c_int64)]
+
+
+EXPORTS = ("puck_default_options", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
+           "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
+           "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
+           "puck_parser_stats", "puck_last_error")
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(build: bool = True) -> ctypes.CDLL:
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.build() if build else _build.LIB
+        if not os.path.exists(path):
+            raise RuntimeError(f"libpuck_gb300.so missing at {path}; run puck_gb300.build.build()")
+        L = ctypes.CDLL(path)
+        P, I, I64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64
+        L.puck_default_options.argtypes = [ctypes.POINTER(Options)]
+        L.puck_grammar_load.restype = P
+        L.puck_grammar_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(I)]
+        L.puck_grammar_free.argtypes = [P]
+        L.puck_grammar_num_levels.argtypes = [P]
+        L.puck_grammar_num_levels.restype = I
+        L.puck_grammar_level_info.argtypes = [P, I, ctypes.POINTER(I)]
+        L.puck_grammar_level_info.restype = I
+        L.puck_grammar_word_id.argtypes = [P, ctypes.c_char_p]
+        L.puck_grammar_word_id.restype = I
+        L.puck_parser_create.restype = P
+        L.puck_parser_create.argtypes = [P, ctypes.POINTER(Options), ctypes.POINTER(I)]
+        L.puck_parser_destroy.argtypes = [P]
+        L.puck_parse.argtypes = [P, P, P, I, P, P]
+        L.puck_parse.restype = I
+        L.puck_partitions.argtypes = [P, P, P, I, P, P]
+        L.puck_partitions.restype = I
+        L.puck_inside_outside.argtypes = [P, P, P, I]
+        L.puck_inside_outside.restype = I
+        L.puck_debug_copy.argtypes = [P, I, I, P, ctypes.c_size_t]
+        L.puck_debug_copy.restype = I
+        L.puck_debug_num_cells.argtypes = [P]
+        L.puck_debug_num_cells.restype = I64
+        L.puck_parser_stats.argtypes = [P, ctypes.POINTER(Stats)]
+        L.puck_parser_stats.restype = I
+        L.puck_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
+        L.puck_last_error.restype = ctypes.c_size_t
+        _lib = L
+        return L
+
+
+def last_error() -> str:
+    L = load()
+    buf = ctypes.create_string_buffer(4096)
+    L.puck_last_error(buf, 4096)
+    return buf.value.decode("utf-8", "replace")
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise PuckError(status, last_error())

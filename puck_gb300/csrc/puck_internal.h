@@ -1,0 +1,111 @@
+// Internal device-side structures of libpuck_gb300 (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace puck {
+
+enum { SEMI_VITERBI = 0, SEMI_REAL = 1, SEMI_LOGSUM = 2 };
+
+// Binary gather jobs.  Inside jobs have the rule parent as target; outside
+// jobs use the reference's rotated rules (the updated child is the target).
+enum JobId { IN_NN, IN_NT, IN_TN, IN_TT, OUT_L_NN, OUT_R_NN, OUT_L_NT, OUT_R_NT,
+             OUT_L_TN, OUT_R_TN, OUT_L_TT, OUT_R_TT, NJOBS };
+enum UJobId { IN_NU, IN_TU, OUT_NU, OUT_TU, NUJOBS };
+
+constexpr int kMaxMask = 8;        // up to 256 coarse symbols
+constexpr int kMaxSplitChunk = 32;  // splits staged in shared memory at once
+constexpr int kMaxLen = 256;        // longest sentence a parser accepts
+
+// A job's rules in CSR over target symbols.  rules[k] = {a | b << 16, bits(w)}
+// with value = (A[a] + B[b]) + w (Viterbi) or A[a] * B[b] * w (Real).
+struct DevJob {
+  int n_tgt;
+  int nseg;
+  const int* rowptr;    // [n_tgt + 1]
+  const int2* rules;    // [rowptr[n_tgt]]
+  const int* tgt_seg;   // [n_tgt] segment of the target's rules, -1 if none
+  const int* seg_bits;  // [nseg * mask_size] coarse-parent bitset of each segment
+};
+
+struct DevUJob {
+  int n_tgt;
+  const int* rowptr;    // [n_tgt + 1]
+  const int2* rules;    // {src, bits(w)}
+};
+
+struct DevLevel {
+  int semiring, n_nt, n_t, cell_size, mask_size, n_coarse, root, num_syms, n_words;
+  int gate_merged;  // non-final level of a cascade: every target gated by segment 0's bits
+  const int* nt_coarse;
+  const int* t_coarse;
+  DevJob jobs[NJOBS];
+  DevUJob ujobs[NUJOBS];
+  const long long* lex_off;
+  const int* lex_term;
+  const float* lex_score;
+  const int* v_off;
+  const int* v_left;
+  const int* v_right;
+  const float* v_score;
+};
+
+// One batch of sentences laid out like the reference's Batch
+// (src/main/scala/puck/parser/Batch.scala:218-253): per sentence a bot half
+// then a top half of n(n+1)/2 cells each, cells in span-major chartIndex order.
+struct DevBatch {
+  int nsent;
+  int max_len;
+  long long num_cells;
+  long long num_tokens;
+  const int* len;             // [nsent]
+  const long long* cell_off;  // [nsent + 1]
+  const long long* word_off;  // [nsent + 1]
+  const int* words;           // [num_tokens]
+  const int* order;           // sentence ids sorted by length, longest first
+  const int* span_pref;       // per span L: prefix sums of (len - L + 1) over order[0..k_L)
+  const int* span_base;       // [max_len + 2] offset of span L's prefix array
+  const int* span_count;      // [max_len + 2] k_L = number of sentences with len >= L
+  const long long* node_off;  // [nsent + 1] first tree node of each sentence
+};
+
+// Pruning mask and log-scales produced by the previous level.
+struct DevMask {
+  const int* bits;      // [num_cells * mask_size] or null (no pruning)
+  int mask_size;
+  const float* iscale;  // [num_cells] or null
+  const float* oscale;
+};
+
+struct DevNode { int top, bot, width; float score; };
+
+// Launch wrappers (kernels.cu).  All return cudaGetLastError() of the launch.
+struct Counters {
+  unsigned long long* corner;   // binary partials >= +0.0 written (the reference drops them)
+  unsigned long long* work;     // (rule, split) applications
+  int* status;                  // per-sentence status codes
+};
+
+cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevMask& M, float* inside,
+                           double* part_scale, Counters C, cudaStream_t st);
+cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
+                               float* inside, Counters C, cudaStream_t st);
+cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
+                                const float* inside, float* outside, Counters C, cudaStream_t st);
+cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
+                         float thresh, int* masks_out, cudaStream_t st);
+cudaError_t launch_scaling(int cell_size, long long num_cells, const float* chart, float* out, cudaStream_t st);
+cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const float* inside, DevNode* nodes,
+                           cudaStream_t st);
+cudaError_t launch_mbr_cells(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
+                             float2* decode, cudaStream_t st);
+cudaError_t launch_mbr_decode(const DevBatch& B, const DevMask& M, int scaling, const float2* decode,
+                              const long long* mbr_off, float* scratch, DevNode* nodes, cudaStream_t st);
+cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevMask& M, const float* inside,
+                               const double* part_scale, float* log_z, cudaStream_t st);
+
+size_t inside_smem_bytes(int cell_size, int chunk);
+int pick_split_chunk(int cell_size, int max_len);
+
+}  // namespace puck

@@ -1,0 +1,892 @@
+// Host runtime of libpuck_gb300: grammar.grz loading, device tables, sentence
+// batching, the coarse-to-fine pass sequence and the C ABI of puck_gpu.h.
+//
+// Orchestration follows the reference's CLParser (dlwh/puck,
+// src/main/scala/puck/parser/CLParser.scala):
+//   parse      = masks from every coarse level, then the last level decodes (:50-53, :145-169)
+//   coarse     = inside, outside, masks at the prune threshold, scales if the next level is Real (:208-250)
+//   partitions = inside of the last level, root scores (:189-206)
+// Batching packs sentences in input order until the chart budget is used
+// (WorkSpace.getBatches, src/main/scala/puck/parser/WorkSpace.scala:20-41);
+// results do not depend on how sentences are batched.
+
+#include "puck_internal.h"
+#include "../../include/puck_gpu.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+struct PuckError {
+  puck_status status;
+  std::string msg;
+};
+
+#define CUDA_TRY(expr)                                                                          \
+  do {                                                                                          \
+    cudaError_t _e = (expr);                                                                    \
+    if (_e != cudaSuccess)                                                                      \
+      throw PuckError{_e == cudaErrorMemoryAllocation ? PUCK_ERR_OOM : PUCK_ERR_CUDA,           \
+                      std::string(#expr) + ": " + cudaGetErrorString(_e)};                      \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// Minimal reader for zip archives with stored (uncompressed) entries.
+struct ZipReader {
+  std::vector<unsigned char> data;
+  std::map<std::string, std::pair<size_t, size_t>> entries;  // name -> (offset, size)
+
+  static uint32_t u32(const unsigned char* p) { return p[0] | (p[1] << 8) | (p[2] << 16) | ((uint32_t)p[3] << 24); }
+  static uint16_t u16(const unsigned char* p) { return (uint16_t)(p[0] | (p[1] << 8)); }
+
+  void open(const std::string& path) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "cannot open " + path};
+    data.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+    if (data.size() < 22) throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": not a zip archive"};
+    size_t eocd = std::string::npos;
+    for (size_t i = data.size() - 22 + 1; i-- > 0 && data.size() - i <= 22 + 65535;) {
+      if (u32(&data[i]) == 0x06054b50u) { eocd = i; break; }
+    }
+    if (eocd == std::string::npos) throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": no end of central directory"};
+    const size_t n = u16(&data[eocd + 10]);
+    size_t cd = u32(&data[eocd + 16]);
+    for (size_t k = 0; k < n; ++k) {
+      if (cd + 46 > data.size() || u32(&data[cd]) != 0x02014b50u)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": corrupt central directory"};
+      const uint16_t method = u16(&data[cd + 10]);
+      const uint32_t csize = u32(&data[cd + 20]);
+      const uint16_t nl = u16(&data[cd + 28]), xl = u16(&data[cd + 30]), cl = u16(&data[cd + 32]);
+      const uint32_t lho = u32(&data[cd + 42]);
+      std::string name(reinterpret_cast<const char*>(&data[cd + 46]), nl);
+      cd += 46 + nl + xl + cl;
+      if (name.size() >= 8 && name.compare(name.size() - 8, 8, ".program") == 0) continue;  // never decoded
+      if (method != 0)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": entry " + name + " is compressed (not a puck_gb300 artifact)"};
+      if (csize == 0xffffffffu || lho == 0xffffffffu)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": zip64 entries are not supported"};
+      if (lho + 30 > data.size() || u32(&data[lho]) != 0x04034b50u)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": corrupt local header"};
+      const size_t start = lho + 30 + u16(&data[lho + 26]) + u16(&data[lho + 28]);
+      if (start + csize > data.size()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": truncated entry " + name};
+      entries[name] = {start, csize};
+    }
+  }
+  bool has(const std::string& name) const { return entries.count(name) != 0; }
+  std::string text(const std::string& name) const {
+    auto it = entries.find(name);
+    if (it == entries.end()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "missing entry " + name};
+    return std::string(reinterpret_cast<const char*>(&data[it->second.first]), it->second.second);
+  }
+};
+
+struct Array {
+  char tag[5] = {0};
+  std::vector<char> bytes;
+  int64_t count = 0;
+};
+
+struct HostLevel {
+  int semiring = 0, n_nt = 0, n_t = 0, cell_size = 0, mask_size = 0, n_coarse = 0, root = 0, n_words = 0;
+  std::map<std::string, Array> arrays;
+  std::vector<std::string> words;
+
+  template <class T>
+  const T* get(const std::string& name, const char* tag, int64_t* count) const {
+    auto it = arrays.find(name);
+    if (it == arrays.end()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "missing array " + name};
+    if (std::strncmp(it->second.tag, tag, 2) != 0) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad dtype for " + name};
+    if (count) *count = it->second.count;
+    return reinterpret_cast<const T*>(it->second.bytes.data());
+  }
+};
+
+std::vector<std::string> split_lines(const std::string& s) {
+  std::vector<std::string> out;
+  size_t i = 0;
+  while (i <= s.size()) {
+    size_t j = s.find('\n', i);
+    if (j == std::string::npos) j = s.size();
+    out.push_back(s.substr(i, j - i));
+    i = j + 1;
+  }
+  return out;
+}
+
+}  // namespace
+
+struct puck_grammar {
+  std::vector<HostLevel> levels;
+  std::unordered_map<std::string, int> word_index;
+};
+
+namespace {
+
+const char* kJobNames[puck::NJOBS] = {"in_NN", "in_NT", "in_TN", "in_TT", "out_L_NN", "out_R_NN",
+                                      "out_L_NT", "out_R_NT", "out_L_TN", "out_R_TN", "out_L_TT", "out_R_TT"};
+const char* kUJobNames[puck::NUJOBS] = {"in_NU", "in_TU", "out_NU", "out_TU"};
+
+// Checks every array the device passes read: presence, dtype, sizes and
+// index ranges (the kernels index shared memory with these values).
+void validate_level(const HostLevel& L) {
+  auto need = [&](const std::string& n, const char* tag, int64_t count) {
+    int64_t c = 0;
+    L.get<char>(n, tag, &c);
+    if (count >= 0 && c != count) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "wrong size for " + n};
+    return c;
+  };
+  auto range = [&](const std::string& n, int64_t hi) {
+    int64_t c = 0;
+    const int* v = L.get<int>(n, "i4", &c);
+    for (int64_t k = 0; k < c; ++k)
+      if (v[k] < 0 || v[k] >= hi) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "index out of range in " + n};
+  };
+  need("nt_coarse", "i4", L.n_nt);
+  need("t_coarse", "i4", L.n_t);
+  range("nt_coarse", L.n_coarse);
+  range("t_coarse", L.n_coarse);
+  if (L.root < 0 || L.root >= L.n_nt) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "root out of range"};
+  static const bool tgt_t[puck::NJOBS] = {false, false, false, false, false, false, false, true, true, false, true, true};
+  static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
+  static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
+  for (int j = 0; j < puck::NJOBS; ++j) {
+    const std::string n = kJobNames[j];
+    const int ntgt = tgt_t[j] ? L.n_t : L.n_nt;
+    const int64_t nr = need(n + "/rowptr", "i4", ntgt + 1);
+    const int* rp = L.get<int>(n + "/rowptr", "i4", nullptr);
+    const int64_t nab = need(n + "/ab", "i4", -1);
+    need(n + "/w", "f4", nab);
+    if (rp[0] != 0 || rp[nr - 1] != nab) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad rowptr for " + n};
+    for (int64_t k = 0; k + 1 < nr; ++k)
+      if (rp[k + 1] < rp[k]) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad rowptr for " + n};
+    const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
+    const int amax = a_t[j] ? L.n_t : L.n_nt, bmax = b_t[j] ? L.n_t : L.n_nt;
+    for (int64_t k = 0; k < nab; ++k) {
+      const int a = ab[k] & 0xffff, b = (int)((unsigned)ab[k] >> 16);
+      if (a >= amax || b >= bmax) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "rule index out of range in " + n};
+    }
+    const int64_t nbits = need(n + "/seg_bits", "i4", -1);
+    if (L.mask_size <= 0 || nbits % L.mask_size) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad seg_bits for " + n};
+    need(n + "/tgt_seg", "i4", ntgt);
+    int64_t c = 0;
+    const int* ts = L.get<int>(n + "/tgt_seg", "i4", &c);
+    for (int64_t k = 0; k < c; ++k)
+      if (ts[k] < -1 || ts[k] >= nbits / L.mask_size) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad tgt_seg in " + n};
+  }
+  static const bool ut[puck::NUJOBS] = {false, false, false, true};
+  static const bool us[puck::NUJOBS] = {false, true, false, false};
+  for (int j = 0; j < puck::NUJOBS; ++j) {
+    const std::string n = kUJobNames[j];
+    const int64_t nr = need(n + "/rowptr", "i4", (ut[j] ? L.n_t : L.n_nt) + 1);
+    const int* rp = L.get<int>(n + "/rowptr", "i4", nullptr);
+    const int64_t ns = need(n + "/src", "i4", rp[nr - 1]);
+    need(n + "/w", "f4", ns);
+    range(n + "/src", us[j] ? L.n_t : L.n_nt);
+  }
+  const int64_t nlo = need("lex_off", "i8", L.n_words + 1);
+  const long long* lo = L.get<long long>("lex_off", "i8", nullptr);
+  need("lex_term", "i4", lo[nlo - 1]);
+  need("lex_score", "f4", lo[nlo - 1]);
+  range("lex_term", L.n_t);
+  const int64_t nvo = need("v_off", "i4", 6LL * L.n_nt + 1);
+  const int* vo = L.get<int>("v_off", "i4", nullptr);
+  need("v_left", "i4", vo[nvo - 1]);
+  need("v_score", "f4", vo[nvo - 1]);
+  need("v_right", "i4", vo[nvo - 1]);
+}
+
+void load_grammar(puck_grammar* g, const std::string& path) {
+  ZipReader z;
+  z.open(path);
+  std::vector<std::string> names;
+  for (auto& l : split_lines(z.text("parserNames")))
+    if (!l.empty()) names.push_back(l);
+  if (names.empty()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": no levels"};
+  for (auto& n : names) {
+    if (!z.has(n + "/header"))
+      throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": level " + n +
+                                                " has no header (reference archives with serialised objects are not decoded)"};
+    HostLevel L;
+    std::map<std::string, std::string> hdr;
+    for (auto& line : split_lines(z.text(n + "/header"))) {
+      size_t sp = line.find(' ');
+      if (sp != std::string::npos) hdr[line.substr(0, sp)] = line.substr(sp + 1);
+    }
+    auto geti = [&](const char* k) {
+      auto it = hdr.find(k);
+      if (it == hdr.end()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, std::string("header lacks ") + k};
+      return std::stoi(it->second);
+    };
+    const std::string sr = hdr["semiring"];
+    L.semiring = sr == "viterbi" ? 0 : sr == "real" ? 1 : sr == "logsum" ? 2 : -1;
+    if (L.semiring < 0) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "unknown semiring " + sr};
+    L.n_nt = geti("n_nt");
+    L.n_t = geti("n_t");
+    L.cell_size = geti("cell_size");
+    L.mask_size = geti("mask_size");
+    L.n_coarse = geti("n_coarse");
+    L.root = geti("root");
+    L.n_words = geti("n_words");
+    if (L.mask_size > puck::kMaxMask) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "too many coarse symbols"};
+    if (L.cell_size % 32 != 0 || L.cell_size < std::max(L.n_nt, L.n_t))
+      throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad cell size"};
+    if (std::max(L.n_nt, L.n_t) > 65535) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "more than 65535 symbols"};
+    const std::string pre = n + "/arrays/";
+    for (auto& e : z.entries) {
+      if (e.first.compare(0, pre.size(), pre) != 0) continue;
+      const unsigned char* p = &z.data[e.second.first];
+      if (e.second.second < 16 || std::memcmp(p, "PKA1", 4) != 0)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad array entry " + e.first};
+      Array a;
+      std::memcpy(a.tag, p + 4, 4);
+      std::memcpy(&a.count, p + 8, 8);
+      size_t esz = (std::strncmp(a.tag, "i8", 2) == 0) ? 8 : 4;
+      if (16 + a.count * esz > e.second.second) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "truncated " + e.first};
+      a.bytes.assign(p + 16, p + 16 + a.count * esz);
+      L.arrays[e.first.substr(pre.size())] = std::move(a);
+    }
+    L.words = split_lines(z.text(n + "/words.txt"));
+    if ((int)L.words.size() != L.n_words) {
+      if (!(L.n_words == 0 && L.words.size() == 1)) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "word list size mismatch"};
+      L.words.clear();
+    }
+    validate_level(L);
+    g->levels.push_back(std::move(L));
+  }
+  const HostLevel& fine = g->levels.back();
+  for (size_t i = 0; i < fine.words.size(); ++i) g->word_index.emplace(fine.words[i], (int)i);
+  for (auto& L : g->levels)
+    if (L.mask_size != g->levels.back().mask_size)
+      throw PuckError{PUCK_ERR_BAD_GRAMMAR, "cascade levels disagree on the coarse symbol set"};
+}
+
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes + bytes / 8, 256);
+    CUDA_TRY(cudaMalloc(&p, want));
+    cap = want;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+struct LevelDev {
+  std::vector<void*> allocs;
+  puck::DevLevel d{};
+  void* upload(const void* src, size_t bytes) {
+    void* p = nullptr;
+    CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
+    allocs.push_back(p);
+    if (bytes) CUDA_TRY(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
+    return p;
+  }
+  ~LevelDev() {
+    for (void* p : allocs) cudaFree(p);
+  }
+};
+
+template <class T>
+const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char* tag, int64_t* count = nullptr) {
+  int64_t c = 0;
+  const T* h = L.get<T>(name, tag, &c);
+  if (count) *count = c;
+  return reinterpret_cast<const T*>(D.upload(h, c * sizeof(T)));
+}
+
+void build_level(LevelDev& D, const HostLevel& L, bool merged) {
+  puck::DevLevel& d = D.d;
+  d.semiring = L.semiring;
+  d.n_nt = L.n_nt;
+  d.n_t = L.n_t;
+  d.cell_size = L.cell_size;
+  d.mask_size = L.mask_size;
+  d.n_coarse = L.n_coarse;
+  d.root = L.root;
+  d.num_syms = std::max(L.n_nt, L.n_t);
+  d.n_words = L.n_words;
+  d.gate_merged = merged ? 1 : 0;
+  d.nt_coarse = up<int>(D, L, "nt_coarse", "i4");
+  d.t_coarse = up<int>(D, L, "t_coarse", "i4");
+  for (int j = 0; j < puck::NJOBS; ++j) {
+    const std::string n = kJobNames[j];
+    int64_t nrow = 0, nab = 0, nw = 0, nseg = 0;
+    const int* rowptr_h = L.get<int>(n + "/rowptr", "i4", &nrow);
+    const int* ab = L.get<int>(n + "/ab", "i4", &nab);
+    const float* w = L.get<float>(n + "/w", "f4", &nw);
+    if (nab != nw || nrow < 1 || rowptr_h[nrow - 1] != nab) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "inconsistent job " + n};
+    std::vector<int2> packed(nab);
+    for (int64_t k = 0; k < nab; ++k) {
+      packed[k].x = ab[k];
+      std::memcpy(&packed[k].y, &w[k], 4);
+    }
+    puck::DevJob& J = d.jobs[j];
+    J.n_tgt = (int)(nrow - 1);
+    J.rowptr = up<int>(D, L, n + "/rowptr", "i4");
+    J.rules = reinterpret_cast<const int2*>(D.upload(packed.data(), packed.size() * sizeof(int2)));
+    J.tgt_seg = up<int>(D, L, n + "/tgt_seg", "i4");
+    J.seg_bits = up<int>(D, L, n + "/seg_bits", "i4", &nseg);
+    J.nseg = (int)(nseg / std::max(1, L.mask_size));
+  }
+  for (int j = 0; j < puck::NUJOBS; ++j) {
+    const std::string n = kUJobNames[j];
+    int64_t nrow = 0, ns = 0, nw = 0;
+    L.get<int>(n + "/rowptr", "i4", &nrow);
+    const int* src = L.get<int>(n + "/src", "i4", &ns);
+    const float* w = L.get<float>(n + "/w", "f4", &nw);
+    if (ns != nw) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "inconsistent unary job " + n};
+    std::vector<int2> packed(ns);
+    for (int64_t k = 0; k < ns; ++k) {
+      packed[k].x = src[k];
+      std::memcpy(&packed[k].y, &w[k], 4);
+    }
+    puck::DevUJob& U = d.ujobs[j];
+    U.n_tgt = (int)(nrow - 1);
+    U.rowptr = up<int>(D, L, n + "/rowptr", "i4");
+    U.rules = reinterpret_cast<const int2*>(D.upload(packed.data(), packed.size() * sizeof(int2)));
+  }
+  d.lex_off = up<long long>(D, L, "lex_off", "i8");
+  d.lex_term = up<int>(D, L, "lex_term", "i4");
+  d.lex_score = up<float>(D, L, "lex_score", "f4");
+  d.v_off = up<int>(D, L, "v_off", "i4");
+  d.v_left = up<int>(D, L, "v_left", "i4");
+  d.v_right = up<int>(D, L, "v_right", "i4");
+  d.v_score = up<float>(D, L, "v_score", "f4");
+}
+
+long long tri(int n) { return (long long)n * (n + 1) / 2; }
+
+enum Mode { MODE_PARSE = 0, MODE_PARTITIONS = 1, MODE_INSIDE_OUTSIDE = 2 };
+
+struct LevelBufs {
+  DevBuf inside, outside, masks, iscale, oscale, part, decode;
+};
+
+}  // namespace
+
+struct puck_parser {
+  const puck_grammar* g = nullptr;
+  puck_options opt{};
+  cudaStream_t stream = nullptr;
+  std::vector<std::unique_ptr<LevelDev>> levels;
+  std::vector<LevelBufs> bufs;
+  DevBuf b_len, b_cell_off, b_word_off, b_words, b_order, b_span_pref, b_span_base, b_span_count, b_node_off,
+      b_mbr_off, b_nodes, b_status, b_logz, b_scratch, b_counters;
+  puck::DevBatch last_batch{};
+  int64_t last_num_cells = 0;
+  int last_batches = 0;
+  puck_stats stats{};
+  int64_t budget_bytes = 0;
+  cudaEvent_t ev[8];
+};
+
+namespace {
+
+int64_t bytes_per_cell(const puck_parser* P, Mode mode) {
+  int64_t b = 0;
+  const int nl = (int)P->g->levels.size();
+  for (int l = 0; l < nl; ++l) {
+    const HostLevel& L = P->g->levels[l];
+    const bool last = l == nl - 1;
+    const bool need_out = !last || mode == MODE_INSIDE_OUTSIDE || (mode == MODE_PARSE && L.semiring != 0 &&
+                                                                    P->opt.decode != PUCK_DECODE_VITERBI);
+    b += (int64_t)L.cell_size * 4 * (need_out ? 2 : 1);
+    if (!last) b += (int64_t)L.mask_size * 4 + 8;
+    else b += 8;
+  }
+  return b;
+}
+
+struct BatchPlan {
+  std::vector<int> sent;  // global sentence ids
+};
+
+void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* word_ids, const int64_t* offsets,
+               puck_tree_node* nodes_out, const std::vector<int64_t>& node_off_global, float* log_z,
+               int32_t* sent_status) {
+  const int nl = (int)P->g->levels.size();
+  cudaStream_t st = P->stream;
+  const int ns = (int)plan.sent.size();
+  // host batch arrays
+  std::vector<int> len(ns);
+  std::vector<long long> cell_off(ns + 1, 0), word_off(ns + 1, 0), node_off(ns + 1, 0), mbr_off(ns + 1, 0);
+  std::vector<int> words;
+  int max_len = 0;
+  for (int i = 0; i < ns; ++i) {
+    const int s = plan.sent[i];
+    len[i] = (int)(offsets[s + 1] - offsets[s]);
+    max_len = std::max(max_len, len[i]);
+    cell_off[i + 1] = cell_off[i] + 2 * tri(len[i]);
+    word_off[i + 1] = word_off[i] + len[i];
+    node_off[i + 1] = node_off[i] + 2 * len[i] - 1;
+    mbr_off[i + 1] = mbr_off[i] + 3LL * (len[i] + 1) * (len[i] + 1);
+    words.insert(words.end(), word_ids + offsets[s], word_ids + offsets[s + 1]);
+  }
+  std::vector<int> order(ns);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return len[a] > len[b]; });
+  std::vector<int> span_pref, span_base(max_len + 2, 0), span_count(max_len + 2, 0), span_cells(max_len + 2, 0);
+  for (int L = 1; L <= max_len; ++L) {
+    span_base[L] = (int)span_pref.size();
+    int k = 0;
+    while (k < ns && len[order[k]] >= L) ++k;
+    span_count[L] = k;
+    int acc = 0;
+    span_pref.push_back(0);
+    for (int j = 0; j < k; ++j) {
+      acc += len[order[j]] - L + 1;
+      span_pref.push_back(acc);
+    }
+    span_cells[L] = acc;
+  }
+  span_base[max_len + 1] = (int)span_pref.size();
+  const long long num_cells = cell_off[ns];
+  auto h2d = [&](DevBuf& b, const void* src, size_t bytes) {
+    b.ensure(std::max<size_t>(bytes, 16));
+    if (bytes) CUDA_TRY(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, st));
+  };
+  h2d(P->b_len, len.data(), ns * sizeof(int));
+  h2d(P->b_cell_off, cell_off.data(), (ns + 1) * sizeof(long long));
+  h2d(P->b_word_off, word_off.data(), (ns + 1) * sizeof(long long));
+  h2d(P->b_words, words.data(), words.size() * sizeof(int));
+  h2d(P->b_order, order.data(), ns * sizeof(int));
+  h2d(P->b_span_pref, span_pref.data(), span_pref.size() * sizeof(int));
+  h2d(P->b_span_base, span_base.data(), span_base.size() * sizeof(int));
+  h2d(P->b_span_count, span_count.data(), span_count.size() * sizeof(int));
+  h2d(P->b_node_off, node_off.data(), (ns + 1) * sizeof(long long));
+  puck::DevBatch B{};
+  B.nsent = ns;
+  B.max_len = max_len;
+  B.num_cells = num_cells;
+  B.num_tokens = word_off[ns];
+  B.len = P->b_len.as<int>();
+  B.cell_off = P->b_cell_off.as<long long>();
+  B.word_off = P->b_word_off.as<long long>();
+  B.words = P->b_words.as<int>();
+  B.order = P->b_order.as<int>();
+  B.span_pref = P->b_span_pref.as<int>();
+  B.span_base = P->b_span_base.as<int>();
+  B.span_count = P->b_span_count.as<int>();
+  B.node_off = P->b_node_off.as<long long>();
+  P->b_status.ensure(ns * sizeof(int) + 16);
+  CUDA_TRY(cudaMemsetAsync(P->b_status.p, 0, ns * sizeof(int), st));
+  P->b_counters.ensure(64);
+  CUDA_TRY(cudaMemsetAsync(P->b_counters.p, 0, 64, st));
+  puck::Counters C{P->b_counters.as<unsigned long long>(), P->b_counters.as<unsigned long long>() + 1,
+                   P->b_status.as<int>()};
+
+  const bool prof = P->opt.profile != 0;
+  auto mark = [&](int i) {
+    if (prof) CUDA_TRY(cudaEventRecord(P->ev[i], st));
+  };
+  double ms_in = 0, ms_out = 0, ms_mask = 0, ms_dec = 0;
+  auto elapsed = [&](int a, int b) {
+    if (!prof) return 0.0;
+    CUDA_TRY(cudaEventSynchronize(P->ev[b]));
+    float ms = 0;
+    CUDA_TRY(cudaEventElapsedTime(&ms, P->ev[a], P->ev[b]));
+    return (double)ms;
+  };
+
+  puck::DevMask M{nullptr, 0, nullptr, nullptr};
+  int64_t launches = 0;
+  for (int l = 0; l < nl; ++l) {
+    const puck::DevLevel& D = P->levels[l]->d;
+    const HostLevel& HL = P->g->levels[l];
+    LevelBufs& lb = P->bufs[l];
+    const bool last = l == nl - 1;
+    const bool need_out = !last || mode == MODE_INSIDE_OUTSIDE ||
+                          (mode == MODE_PARSE && HL.semiring != 0 && P->opt.decode != PUCK_DECODE_VITERBI);
+    lb.inside.ensure(num_cells * D.cell_size * sizeof(float));
+    if (need_out) lb.outside.ensure(num_cells * D.cell_size * sizeof(float));
+    lb.part.ensure(ns * sizeof(double) + 16);
+    CUDA_TRY(cudaMemsetAsync(lb.part.p, 0, ns * sizeof(double), st));
+    float* inside = lb.inside.as<float>();
+    float* outside = need_out ? lb.outside.as<float>() : nullptr;
+    puck::DevMask MM = M;
+    if (D.semiring != puck::SEMI_REAL) { MM.iscale = nullptr; MM.oscale = nullptr; }
+    mark(0);
+    CUDA_TRY(puck::launch_lexicon(D, B, MM, inside, lb.part.as<double>(), C, st));
+    ++launches;
+    for (int span = 1; span <= max_len; ++span) {
+      CUDA_TRY(puck::launch_inside_span(D, B, MM, span, span_cells[span], inside, C, st));
+      ++launches;
+    }
+    mark(1);
+    if (need_out) {
+      for (int span = max_len; span >= 1; --span) {
+        CUDA_TRY(puck::launch_outside_span(D, B, MM, span, span_cells[span], inside, outside, C, st));
+        ++launches;
+      }
+    }
+    mark(2);
+    ms_in += elapsed(0, 1);
+    ms_out += elapsed(1, 2);
+    if (!last) {
+      lb.masks.ensure(num_cells * D.mask_size * sizeof(int));
+      CUDA_TRY(puck::launch_masks(D, B, inside, outside, P->opt.prune_threshold, lb.masks.as<int>(), st));
+      ++launches;
+      lb.iscale.ensure(num_cells * sizeof(float));
+      lb.oscale.ensure(num_cells * sizeof(float));
+      const bool next_real = P->g->levels[l + 1].semiring == puck::SEMI_REAL;
+      if (next_real) {
+        CUDA_TRY(puck::launch_scaling(D.cell_size, num_cells, inside, lb.iscale.as<float>(), st));
+        CUDA_TRY(puck::launch_scaling(D.cell_size, num_cells, outside, lb.oscale.as<float>(), st));
+        launches += 2;
+      } else {
+        CUDA_TRY(cudaMemsetAsync(lb.iscale.p, 0, num_cells * sizeof(float), st));
+        CUDA_TRY(cudaMemsetAsync(lb.oscale.p, 0, num_cells * sizeof(float), st));
+      }
+      mark(3);
+      ms_mask += elapsed(2, 3);
+      M.bits = lb.masks.as<int>();
+      M.mask_size = D.mask_size;
+      M.iscale = lb.iscale.as<float>();
+      M.oscale = lb.oscale.as<float>();
+      continue;
+    }
+    // last level
+    mark(4);
+    if (mode == MODE_PARTITIONS) {
+      P->b_logz.ensure(ns * sizeof(float) + 16);
+      CUDA_TRY(puck::launch_root_scores(D, B, MM, inside, lb.part.as<double>(), P->b_logz.as<float>(), st));
+      ++launches;
+      std::vector<float> lz(ns);
+      CUDA_TRY(cudaMemcpyAsync(lz.data(), P->b_logz.p, ns * sizeof(float), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      for (int i = 0; i < ns; ++i) log_z[plan.sent[i]] = lz[i];
+    } else if (mode == MODE_PARSE) {
+      P->b_nodes.ensure(node_off[ns] * sizeof(puck::DevNode) + 16);
+      const bool vit = P->opt.decode == PUCK_DECODE_VITERBI ||
+                       (P->opt.decode == PUCK_DECODE_AUTO && D.semiring == puck::SEMI_VITERBI);
+      if (vit) {
+        if (D.semiring != puck::SEMI_VITERBI)
+          throw PuckError{PUCK_ERR_INVALID_ARG, "Viterbi decoding needs a Viterbi fine level"};
+        CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
+        ++launches;
+      } else {
+        if (!M.bits) throw PuckError{PUCK_ERR_INVALID_ARG, "Can't use null pruning mask for parse extraction!"};
+        if (D.semiring == puck::SEMI_VITERBI)
+          throw PuckError{PUCK_ERR_INVALID_ARG, "MBR decoding needs a sum-product fine level"};
+        lb.decode.ensure(num_cells * sizeof(float2));
+        CUDA_TRY(puck::launch_mbr_cells(D, B, inside, outside, lb.decode.as<float2>(), st));
+        h2d(P->b_mbr_off, mbr_off.data(), (ns + 1) * sizeof(long long));
+        P->b_scratch.ensure(mbr_off[ns] * sizeof(float) + 16);
+        CUDA_TRY(puck::launch_mbr_decode(B, M, D.semiring == puck::SEMI_REAL ? 1 : 0, lb.decode.as<float2>(),
+                                         P->b_mbr_off.as<long long>(), P->b_scratch.as<float>(),
+                                         P->b_nodes.as<puck::DevNode>(), st));
+        launches += 2;
+      }
+      std::vector<puck::DevNode> hn(node_off[ns]);
+      CUDA_TRY(cudaMemcpyAsync(hn.data(), P->b_nodes.p, hn.size() * sizeof(puck::DevNode), cudaMemcpyDeviceToHost, st));
+      CUDA_TRY(cudaStreamSynchronize(st));
+      for (int i = 0; i < ns; ++i) {
+        const int s = plan.sent[i];
+        std::memcpy(nodes_out + node_off_global[s], hn.data() + node_off[i],
+                    (2 * len[i] - 1) * sizeof(puck_tree_node));
+      }
+    } else {
+      if (!last || true) {
+        if (D.semiring == puck::SEMI_VITERBI) {
+          P->b_nodes.ensure(node_off[ns] * sizeof(puck::DevNode) + 16);
+          CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
+        } else {
+          lb.decode.ensure(num_cells * sizeof(float2));
+          CUDA_TRY(puck::launch_mbr_cells(D, B, inside, outside, lb.decode.as<float2>(), st));
+        }
+        ++launches;
+      }
+    }
+    mark(5);
+    ms_dec += elapsed(4, 5);
+  }
+  std::vector<int> status(ns);
+  unsigned long long ctr[2] = {0, 0};
+  CUDA_TRY(cudaMemcpyAsync(status.data(), P->b_status.p, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(ctr, P->b_counters.p, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (sent_status)
+    for (int i = 0; i < ns; ++i)
+      if (status[i]) sent_status[plan.sent[i]] = status[i];
+  P->stats.ms_inside += ms_in;
+  P->stats.ms_outside += ms_out;
+  P->stats.ms_masks += ms_mask;
+  P->stats.ms_decode += ms_dec;
+  P->stats.cells += num_cells;
+  P->stats.binary_work += (int64_t)ctr[1];
+  P->stats.kernel_launches += launches;
+  P->stats.batches += 1;
+  P->last_batch = B;
+  P->last_num_cells = num_cells;
+}
+
+puck_status run_call(puck_parser* P, Mode mode, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                     puck_tree_node* nodes_out, float* log_z, int32_t* sent_status) {
+  try {
+    if (!P || (nsent > 0 && (!word_ids || !offsets))) throw PuckError{PUCK_ERR_INVALID_ARG, "null argument"};
+    if (nsent < 0) throw PuckError{PUCK_ERR_INVALID_ARG, "negative sentence count"};
+    CUDA_TRY(cudaSetDevice(P->opt.device));
+    const auto t0 = std::chrono::steady_clock::now();
+    P->stats = puck_stats{};
+    const int nwords = P->g->levels.back().n_words;
+    std::vector<int64_t> node_off(nsent + 1, 0);
+    std::vector<int> valid;
+    int first_bad = PUCK_OK;
+    for (int s = 0; s < nsent; ++s) {
+      const int64_t n = offsets[s + 1] - offsets[s];
+      node_off[s + 1] = node_off[s] + std::max<int64_t>(2 * n - 1, 0);
+      int st = PUCK_OK;
+      if (n <= 0) st = PUCK_ERR_EMPTY;
+      else if (n > P->opt.max_length) st = PUCK_ERR_SENT_TOO_LONG;
+      else
+        for (int64_t k = offsets[s]; k < offsets[s + 1]; ++k)
+          if (word_ids[k] < 0 || word_ids[k] >= nwords) { st = PUCK_ERR_OOV; break; }
+      if (sent_status) sent_status[s] = st;
+      if (st == PUCK_OK) valid.push_back(s);
+      else if (first_bad == PUCK_OK) first_bad = st;
+    }
+    if (nodes_out && mode == MODE_PARSE) std::memset(nodes_out, 0, node_off[nsent] * sizeof(puck_tree_node));
+    if (log_z && mode == MODE_PARTITIONS)
+      for (int s = 0; s < nsent; ++s) log_z[s] = std::nanf("");
+    const int64_t per_cell = bytes_per_cell(P, mode);
+    const int64_t cap_cells = std::max<int64_t>(P->budget_bytes / std::max<int64_t>(per_cell, 1), 1);
+    std::vector<BatchPlan> plans;
+    BatchPlan cur;
+    int64_t cur_cells = 0;
+    for (int s : valid) {
+      const int64_t c = 2 * tri((int)(offsets[s + 1] - offsets[s]));
+      if (c > cap_cells) {
+        if (sent_status) sent_status[s] = PUCK_ERR_OOM;
+        continue;
+      }
+      if (!cur.sent.empty() && (cur_cells + c > cap_cells ||
+                                (P->opt.max_batch_sentences > 0 && (int)cur.sent.size() >= P->opt.max_batch_sentences))) {
+        plans.push_back(std::move(cur));
+        cur = BatchPlan();
+        cur_cells = 0;
+      }
+      cur.sent.push_back(s);
+      cur_cells += c;
+    }
+    if (!cur.sent.empty()) plans.push_back(std::move(cur));
+    for (auto& pl : plans) run_batch(P, mode, pl, word_ids, offsets, nodes_out, node_off, log_z, sent_status);
+    P->last_batches = (int)plans.size();
+    P->stats.cells_pruned = 0;
+    P->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    (void)first_bad;
+    return PUCK_OK;
+  } catch (const PuckError& e) {
+    set_error(e.msg);
+    return e.status;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return PUCK_ERR_INTERNAL;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+void puck_default_options(puck_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->mem_bytes = 0;
+  o->device = 0;
+  o->profile = 0;
+  o->decode = PUCK_DECODE_AUTO;
+  o->max_length = 100;
+  o->max_batch_sentences = 0;
+  o->prune_threshold = -9.0f;
+  o->use_graphs = 0;
+}
+
+puck_grammar* puck_grammar_load(const char* path, puck_status* status) {
+  auto* g = new puck_grammar();
+  try {
+    if (!path) throw PuckError{PUCK_ERR_INVALID_ARG, "null path"};
+    load_grammar(g, path);
+    if (status) *status = PUCK_OK;
+    return g;
+  } catch (const PuckError& e) {
+    set_error(e.msg);
+    if (status) *status = e.status;
+  } catch (const std::exception& e) {
+    set_error(std::string("grammar load failed: ") + e.what());
+    if (status) *status = PUCK_ERR_BAD_GRAMMAR;
+  }
+  delete g;
+  return nullptr;
+}
+
+void puck_grammar_free(puck_grammar* g) { delete g; }
+
+int32_t puck_grammar_num_levels(const puck_grammar* g) { return g ? (int32_t)g->levels.size() : 0; }
+
+puck_status puck_grammar_level_info(const puck_grammar* g, int32_t level, int32_t out[8]) {
+  if (!g || level < 0 || level >= (int)g->levels.size() || !out) {
+    set_error("bad level");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  const HostLevel& L = g->levels[level];
+  int32_t v[8] = {L.semiring, L.n_nt, L.n_t, L.cell_size, L.mask_size, L.n_coarse, L.root, L.n_words};
+  std::memcpy(out, v, sizeof(v));
+  return PUCK_OK;
+}
+
+int32_t puck_grammar_word_id(const puck_grammar* g, const char* word) {
+  if (!g || !word) return -1;
+  auto it = g->word_index.find(word);
+  return it == g->word_index.end() ? -1 : it->second;
+}
+
+puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts, puck_status* status) {
+  auto* P = new puck_parser();
+  try {
+    if (!g) throw PuckError{PUCK_ERR_INVALID_ARG, "null grammar"};
+    P->g = g;
+    if (opts) P->opt = *opts;
+    else puck_default_options(&P->opt);
+    if (P->opt.max_length <= 0) P->opt.max_length = 100;
+    if (P->opt.max_length > puck::kMaxLen)
+      throw PuckError{PUCK_ERR_INVALID_ARG, "max_length above " + std::to_string(puck::kMaxLen)};
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (P->opt.device < 0 || P->opt.device >= ndev) throw PuckError{PUCK_ERR_INVALID_ARG, "no such CUDA device"};
+    CUDA_TRY(cudaSetDevice(P->opt.device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
+    for (auto& e : P->ev) CUDA_TRY(cudaEventCreate(&e));
+    const int nl = (int)g->levels.size();
+    for (int l = 0; l < nl; ++l) {
+      P->levels.emplace_back(new LevelDev());
+      build_level(*P->levels.back(), g->levels[l], l < nl - 1 && nl != 1);
+    }
+    P->bufs.resize(nl);
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t cap = (int64_t)(free_b * 0.8);
+    P->budget_bytes = P->opt.mem_bytes > 0 ? std::min<int64_t>(P->opt.mem_bytes, cap) : cap;
+    if (status) *status = PUCK_OK;
+    return P;
+  } catch (const PuckError& e) {
+    set_error(e.msg);
+    if (status) *status = e.status;
+  }
+  puck_parser_destroy(P);
+  return nullptr;
+}
+
+void puck_parser_destroy(puck_parser* P) {
+  if (!P) return;
+  cudaSetDevice(P->opt.device);
+  for (auto& b : P->bufs) {
+    b.inside.release(); b.outside.release(); b.masks.release(); b.iscale.release(); b.oscale.release();
+    b.part.release(); b.decode.release();
+  }
+  for (DevBuf* b : {&P->b_len, &P->b_cell_off, &P->b_word_off, &P->b_words, &P->b_order, &P->b_span_pref,
+                    &P->b_span_base, &P->b_span_count, &P->b_node_off, &P->b_mbr_off, &P->b_nodes, &P->b_status,
+                    &P->b_logz, &P->b_scratch, &P->b_counters})
+    b->release();
+  P->levels.clear();
+  for (auto& e : P->ev)
+    if (e) cudaEventDestroy(e);
+  if (P->stream) cudaStreamDestroy(P->stream);
+  delete P;
+}
+
+puck_status puck_parse(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                       puck_tree_node* nodes_out, int32_t* sent_status) {
+  if (!nodes_out && nsent > 0) {
+    set_error("null nodes_out");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  return run_call(p, MODE_PARSE, word_ids, offsets, nsent, nodes_out, nullptr, sent_status);
+}
+
+puck_status puck_partitions(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                            float* log_z, int32_t* sent_status) {
+  if (!log_z && nsent > 0) {
+    set_error("null log_z");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  return run_call(p, MODE_PARTITIONS, word_ids, offsets, nsent, nullptr, log_z, sent_status);
+}
+
+puck_status puck_inside_outside(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent) {
+  return run_call(p, MODE_INSIDE_OUTSIDE, word_ids, offsets, nsent, nullptr, nullptr, nullptr);
+}
+
+int64_t puck_debug_num_cells(const puck_parser* p) { return p ? p->last_num_cells : 0; }
+
+puck_status puck_debug_copy(puck_parser* P, int32_t level, int32_t which, void* host_out, size_t bytes) {
+  try {
+    if (!P || level < 0 || level >= (int)P->bufs.size() || !host_out)
+      throw PuckError{PUCK_ERR_INVALID_ARG, "bad debug copy arguments"};
+    if (P->last_batches != 1) throw PuckError{PUCK_ERR_INVALID_ARG, "last call did not run as one batch"};
+    const HostLevel& L = P->g->levels[level];
+    LevelBufs& b = P->bufs[level];
+    const int64_t nc = P->last_num_cells;
+    const void* src = nullptr;
+    size_t need = 0;
+    switch (which) {
+      case 0: src = b.inside.p; need = nc * L.cell_size * 4; break;
+      case 1: src = b.outside.p; need = nc * L.cell_size * 4; break;
+      case 2: src = b.masks.p; need = nc * L.mask_size * 4; break;
+      case 3: src = b.iscale.p; need = nc * 4; break;
+      case 4: src = b.oscale.p; need = nc * 4; break;
+      case 5: src = b.decode.p; need = nc * 8; break;
+      default: throw PuckError{PUCK_ERR_INVALID_ARG, "bad 'which'"};
+    }
+    if (!src) throw PuckError{PUCK_ERR_INVALID_ARG, "buffer not computed by the last call"};
+    if (bytes < need) throw PuckError{PUCK_ERR_INVALID_ARG, "host buffer too small"};
+    CUDA_TRY(cudaSetDevice(P->opt.device));
+    CUDA_TRY(cudaMemcpyAsync(host_out, src, need, cudaMemcpyDeviceToHost, P->stream));
+    CUDA_TRY(cudaStreamSynchronize(P->stream));
+    return PUCK_OK;
+  } catch (const PuckError& e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}
+
+puck_status puck_parser_stats(const puck_parser* p, puck_stats* out) {
+  if (!p || !out) return PUCK_ERR_INVALID_ARG;
+  *out = p->stats;
+  return PUCK_OK;
+}
+
+size_t puck_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    size_t n = std::min(len - 1, g_last_error.size());
+    std::memcpy(buf, g_last_error.data(), n);
+    buf[n] = 0;
+  }
+  return g_last_error.size();
+}
+
+}  // extern "C"

@@ -1,0 +1,61 @@
+"""Grammar and sentence builders shared by the tests (seeded, cached per process)."""
+from __future__ import annotations
+
+import functools
+import os
+import tempfile
+
+import numpy as np
+
+from puck_gb300 import grammar, grz, synth
+
+_TMP = tempfile.mkdtemp(prefix="puck_tests_")
+
+
+@functools.lru_cache(maxsize=None)
+def small_pcfg_levels(semiring="viterbi"):
+    """The plain 64+32-symbol PCFG, single level."""
+    g = synth.small_pcfg(0)
+    return (grammar.compile_level(g, semiring),)
+
+
+@functools.lru_cache(maxsize=None)
+def tiny_pcfg_levels(semiring="viterbi"):
+    g = synth.small_pcfg(7, n_nt=12, n_pt=6, n_binary=500, n_unary=10, n_words=120)
+    return (grammar.compile_level(g, semiring),)
+
+
+@functools.lru_cache(maxsize=None)
+def split_levels(fine_semiring="viterbi", size="medium"):
+    """Coarse (Viterbi) + fine split grammar cascade."""
+    if size == "medium":
+        c, f = synth.split_grammar(seed=4, n_coarse_nt=10, n_coarse_pt=8, max_split=8, mean_split=6.0,
+                                   n_coarse_rules=120, target_fine_rules=20000, n_coarse_unaries=20, n_words=500)
+    else:
+        c, f = synth.split_grammar(seed=3, n_coarse_nt=8, n_coarse_pt=6, max_split=4, mean_split=3.0,
+                                   n_coarse_rules=60, target_fine_rules=3000, n_coarse_unaries=12, n_words=300)
+    return (grammar.compile_level(c, "viterbi"), grammar.compile_level(f, fine_semiring))
+
+
+def write_grz(levels, name):
+    path = os.path.join(_TMP, name + ".grz")
+    if not os.path.exists(path):
+        grz.write_sequence(path, levels)
+    return path
+
+
+def c0_sentences(n=64, seed=1):
+    return synth.uniform_sentences(seed, n, 5, 20, 5000)
+
+
+def split_sentences(n=48, seed=5, n_words=500, mean=14, hi=30):
+    return synth.lognormal_sentences(seed, n, mean, 1, hi, n_words)
+
+
+def node_blocks(nodes, lengths):
+    out, start = [], 0
+    for n in lengths:
+        k = max(2 * int(n) - 1, 0)
+        out.append(nodes[start:start + k])
+        start += k
+    return out
