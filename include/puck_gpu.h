@@ -73,10 +73,16 @@ typedef struct puck_tree_node {
   float score;
 } puck_tree_node;
 
+/* Counters of the last call.  ms_* are CUDA-event times on the parser's
+ * stream summed over batches: ms_device from the first to the last kernel
+ * of each batch (no host work, no host<->device copies), ms_inside ..
+ * ms_decode per pass kind over all levels. */
 typedef struct puck_stats {
   double ms_total, ms_inside, ms_outside, ms_masks, ms_decode, ms_h2d, ms_d2h;
   int64_t cells, cells_pruned, batches, kernel_launches;
   int64_t binary_work;        /* (rule, split) applications executed in the last call */
+  double ms_device;
+  int64_t h2d_bytes, d2h_bytes;
 } puck_stats;
 
 void puck_default_options(puck_options* opts);
@@ -121,6 +127,11 @@ puck_status puck_debug_copy(puck_parser* p, int32_t level, int32_t which, void* 
 int64_t puck_debug_num_cells(const puck_parser* p);
 
 puck_status puck_parser_stats(const puck_parser* p, puck_stats* out);
+
+/* Per-level pass times of the last call (CUDA events, summed over batches):
+ * out[0] inside, out[1] outside, out[2] masks + scaling, out[3] decode (ms);
+ * launches[0..3] the matching kernel launch counts. */
+puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[4], int64_t launches[4]);
 
 /* Last error message of the calling thread; returns the full length. */
 size_t puck_last_error(char* buf, size_t len);

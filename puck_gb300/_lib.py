@@ -38,13 +38,14 @@ class Stats(ctypes.Structure):
     _fields_ = [("ms_total", ctypes.c_double), ("ms_inside", ctypes.c_double), ("ms_outside", ctypes.c_double),
                 ("ms_masks", ctypes.c_double), ("ms_decode", ctypes.c_double), ("ms_h2d", ctypes.c_double),
                 ("ms_d2h", ctypes.c_double), ("cells", ctypes.c_int64), ("cells_pruned", ctypes.c_int64),
-                ("batches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("binary_work", ctypes.c_int64)]
+                ("batches", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("binary_work", ctypes.c_int64),
+                ("ms_device", ctypes.c_double), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
 
 EXPORTS = ("puck_default_options", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
            "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
-           "puck_parser_stats", "puck_last_error")
+           "puck_parser_stats", "puck_parser_pass_ms", "puck_last_error")
 
 _lib = None
 _lock = threading.Lock()
@@ -85,6 +86,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_debug_num_cells.restype = I64
         L.puck_parser_stats.argtypes = [P, ctypes.POINTER(Stats)]
         L.puck_parser_stats.restype = I
+        L.puck_parser_pass_ms.argtypes = [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(I64)]
+        L.puck_parser_pass_ms.restype = I
         L.puck_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         L.puck_last_error.restype = ctypes.c_size_t
         _lib = L

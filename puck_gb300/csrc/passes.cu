@@ -1,0 +1,708 @@
+// Chart passes of the hot path on sm_103a: lexicon, inside and outside span
+// wavefronts (binary rules + unary layer).
+//
+// One CTA owns one target cell of a span-length wavefront and reduces every
+// rule application into it in *gather* form, so there are no global atomics
+// and the cell is written exactly once.  Max-plus (Viterbi) cells are
+// bit-identical to the reference's per-rule ``max(p, (L + R) + w)``
+// (SimpleGenRuleMultiply.java:151) because x -> fl(x + w) is monotone:
+//     max_s fl(fl(L_s + R_s) + w) == fl(max_s fl(L_s + R_s) + w).
+//
+// Split grammars use the pair-factored form.  Rules are grouped by the coarse
+// projection (Y, Z) of their operands.  For a target cell, a warp computes the
+// max-plus outer product M[j][k] = max_s A_s[Y_j] + B_s[Z_k] over the splits s
+// once per pair, then applies every rule of the pair as M[j][k] + w.  Both
+// steps are exact in max-plus arithmetic.  Every producing kernel records, per
+// cell, which coarse symbols hold a non-zero value (its liveness bitset).  A
+// pair is skipped for a split whose left operand has no live Y or right operand
+// no live Z.  This is exact too, because every skipped term is the semiring
+// zero.  Operand values are read through L1, so the pass needs little shared
+// memory and several CTAs share an SM.  Grammars without split structure keep
+// target-major rule scans over operand cells staged in shared memory.
+//
+// Reference semantics restated (dlwh/puck paths):
+//   gating        CLParser.scala:845-855,885-901 (segment bits vs cell mask, child "any")
+//   inside pass   CLParser.scala:256-314,489-504
+//   outside pass  CLParser.scala:316-369,506-522
+//   unaries       CLParser.scala:698-763, SimpleGenRuleMultiply.java:255-319
+//   lexicon       CLParser.scala:411-467
+
+#include "device_common.cuh"
+
+namespace puck {
+namespace {
+
+using namespace dev;
+
+constexpr int kPairChunk = 64;   // splits per liveness chunk (two ballots)
+constexpr int kThreads = 256;
+
+// Shared bookkeeping of one target cell.
+struct CellCtx {
+  const float* aptr[kMaxLen];   // operand cells of each allowed split
+  const float* bptr[kMaxLen];
+  const int* alive[kMaxLen];    // their liveness words
+  const int* blive[kMaxLen];
+  float scl[kMaxLen];           // Real semiring: per-split scale exp(-p + l + r)
+  int la[kPairChunk][kMaxMask];
+  int lb[kPairChunk][kMaxMask];
+  int gate[kMaxMask];
+  unsigned words[kMaxMask];
+  int nsp, nlive;
+  int flag0, flag1;
+  unsigned long long work, corner;
+};
+
+// Dynamic shared memory of a pass kernel: [P | Q | mode 0: staged operand
+// cells | mode 2: per-warp outer-product tiles, pair liveness, live list].
+struct Smem {
+  float* P;
+  float* Q;
+  float* stA;
+  float* stB;
+  float* M;
+  unsigned* pl;
+  int* list;
+};
+
+__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk) {
+  Smem m;
+  const int cs = L.cell_size;
+  m.P = base;
+  m.Q = base + cs;
+  float* rest = base + 2 * cs;
+  m.stA = m.stB = m.M = nullptr;
+  m.pl = nullptr;
+  m.list = nullptr;
+  if (L.mode == 2) {
+    m.M = rest;
+    m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * L.max_mtile);
+    m.list = reinterpret_cast<int*>(m.pl + L.n_coarse * L.mask_size);
+  } else {
+    m.stA = rest;
+    m.stB = rest + chunk * cs;
+  }
+  return m;
+}
+
+// float max through integer atomics (valid for every non-NaN value)
+__device__ __forceinline__ void atomic_fmax(float* addr, float v) {
+  if (__float_as_int(v) >= 0) atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+  else atomicMin(reinterpret_cast<unsigned*>(addr), __float_as_uint(v));
+}
+
+template <int S>
+__device__ __forceinline__ void add_split(CellCtx& X, const float* a, const float* b, const int* la,
+                                          const int* lb, float ls, float rs, float ps) {
+  int k = X.nsp++;
+  X.aptr[k] = a;
+  X.bptr[k] = b;
+  X.alive[k] = la;
+  X.blive[k] = lb;
+  if (S == SEMI_REAL) X.scl[k] = __expf(-ps + rs + ls);
+}
+
+__device__ __forceinline__ void stage(CellCtx& X, int c0, int nc, int cs, float* stA, float* stB) {
+  const int n4 = cs >> 2;
+  for (int idx = threadIdx.x; idx < nc * n4; idx += blockDim.x) {
+    const int s = idx / n4, k = idx - s * n4;
+    reinterpret_cast<float4*>(stA + s * cs)[k] = __ldg(reinterpret_cast<const float4*>(X.aptr[c0 + s]) + k);
+    reinterpret_cast<float4*>(stB + s * cs)[k] = __ldg(reinterpret_cast<const float4*>(X.bptr[c0 + s]) + k);
+  }
+}
+
+__device__ __forceinline__ bool gate_hit(const DevJob& J, int seg, int ms, int merged, const int* gate) {
+  const int* bits = J.seg_bits + (merged ? 0 : seg) * ms;
+  bool hit = false;
+  for (int i = 0; i < ms; ++i) hit |= (__ldg(bits + i) & gate[i]) != 0;
+  return hit;
+}
+
+// Target-major layout: one warp per target symbol, lanes over its rules.
+template <int S>
+__device__ void gather_targets(const DevJob& J, const DevLevel& L, bool gated, float* P, float* stA, float* stB,
+                               int chunk, CellCtx& X) {
+  const int cs = L.cell_size, ms = L.mask_size;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int nsp = X.nsp;
+  unsigned long long work = 0, corner = 0;
+  for (int c0 = 0; c0 < nsp; c0 += chunk) {
+    const int nc = min(chunk, nsp - c0);
+    stage(X, c0, nc, cs, stA, stB);
+    __syncthreads();
+    for (int t = warp; t < J.n_tgt; t += nwarps) {
+      const int seg = __ldg(J.tgt_seg + t);
+      if (seg < 0) continue;
+      if (gated && !gate_hit(J, seg, ms, L.gate_merged, X.gate)) continue;
+      const int r0 = __ldg(J.rowptr + t), r1 = __ldg(J.rowptr + t + 1);
+      float acc = Sr<S>::zero();
+      for (int r = r0 + lane; r < r1; r += 32) {
+        const int2 rr = __ldg(J.rules + r);
+        const int a = rr.x & 0xffff, b = (int)((unsigned)rr.x >> 16);
+        const float w = __int_as_float(rr.y);
+        if (S == SEMI_VITERBI) {
+          float v = -CUDART_INF_F;
+          for (int s = 0; s < nc; ++s) v = fmaxf(v, stA[s * cs + a] + stB[s * cs + b]);
+          acc = fmaxf(acc, v + w);
+        } else if (S == SEMI_REAL) {
+          float v = 0.f;
+          for (int s = 0; s < nc; ++s) v = fmaf(X.scl[c0 + s], stA[s * cs + a] * stB[s * cs + b], v);
+          acc = fmaf(v, w, acc);
+        } else {
+          float v = Sr<S>::zero();
+          for (int s = 0; s < nc; ++s) v = Sr<S>::add(v, stA[s * cs + a] + stB[s * cs + b]);
+          acc = Sr<S>::add(acc, v + w);
+        }
+      }
+      acc = warp_reduce<S>(acc);
+      if (lane == 0) {
+        P[t] = Sr<S>::add(P[t], acc);
+        work += (unsigned long long)(r1 - r0) * nc;
+        if (S == SEMI_VITERBI && acc >= 0.f) corner++;
+      }
+    }
+    __syncthreads();
+  }
+  if (lane == 0 && (work | corner)) {
+    atomicAdd(&X.work, work);
+    atomicAdd(&X.corner, corner);
+  }
+}
+
+__device__ __forceinline__ bool bit(const int* words, int c) { return (words[c >> 5] >> (c & 31)) & 1; }
+
+template <int S>
+__device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned long long& corner) {
+  if (S == SEMI_VITERBI) {
+    if (v != -CUDART_INF_F) {
+      atomic_fmax(P + t, v);
+      if (v >= 0.f) ++corner;
+    }
+  } else if (v != 0.f) {
+    atomicAdd(P + t, v);
+  }
+}
+
+// Pair-factored gather (level mode 2), see the file comment.
+template <int S>
+__device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
+                             CellCtx& X) {
+  const int ms = L.mask_size, nco = L.n_coarse;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int* aoff = J.a_is_t ? L.t_mem_off : L.nt_mem_off;
+  const int* amem = J.a_is_t ? L.t_mem : L.nt_mem;
+  const int* boff = J.b_is_t ? L.t_mem_off : L.nt_mem_off;
+  const int* bmem = J.b_is_t ? L.t_mem : L.nt_mem;
+  float* Mw = sm.M + warp * L.max_mtile;
+  const int nsp = X.nsp;
+  unsigned long long work = 0, corner = 0;
+  for (int c0 = 0; c0 < nsp; c0 += kPairChunk) {
+    const int nc = min(kPairChunk, nsp - c0);
+    for (int i = threadIdx.x; i < nc * ms; i += blockDim.x) {
+      const int s = i / ms, w = i - s * ms;
+      X.la[s][w] = __ldg(X.alive[c0 + s] + w);
+      X.lb[s][w] = __ldg(X.blive[c0 + s] + w);
+    }
+    if (threadIdx.x == 0) X.nlive = 0;
+    __syncthreads();
+    // pl[ca] = union over splits with a live ca on the left of the right-hand live sets
+    for (int ca = threadIdx.x; ca < nco; ca += blockDim.x) {
+      unsigned acc[kMaxMask];
+#pragma unroll
+      for (int w = 0; w < kMaxMask; ++w) acc[w] = 0u;
+      for (int s = 0; s < nc; ++s) {
+        if (bit(X.la[s], ca)) {
+#pragma unroll
+          for (int w = 0; w < kMaxMask; ++w)
+            if (w < ms) acc[w] |= (unsigned)X.lb[s][w];
+        }
+      }
+#pragma unroll
+      for (int w = 0; w < kMaxMask; ++w)
+        if (w < ms) sm.pl[ca * ms + w] = acc[w];
+    }
+    __syncthreads();
+    // compact the live pairs (coarse liveness, then the OR of their segments' bits)
+    for (int base = 0; base < J.npair; base += blockDim.x) {
+      const int k = base + threadIdx.x;
+      bool live = false;
+      if (k < J.npair) {
+        const int key = __ldg(J.pair_key + k);
+        const int ca = key & 255, cb = (key >> 8) & 255;
+        live = (sm.pl[ca * ms + (cb >> 5)] >> (cb & 31)) & 1u;
+        if (live && gated) {
+          bool hit = false;
+          for (int i = 0; i < ms; ++i) hit |= (__ldg(J.pair_gate + k * ms + i) & X.gate[i]) != 0;
+          live = hit;
+        }
+      }
+      const unsigned bal = __ballot_sync(kFull, live);
+      int wb = 0;
+      if (lane == 0 && bal) wb = atomicAdd(&X.nlive, __popc(bal));
+      wb = __shfl_sync(kFull, wb, 0);
+      if (live) sm.list[wb + __popc(bal & ((1u << lane) - 1u))] = k;
+    }
+    __syncthreads();
+    const int nlive = X.nlive;
+    for (int i = warp; i < nlive; i += nwarps) {
+      const int p = sm.list[i];
+      const int key = __ldg(J.pair_key + p);
+      const int ca = key & 255, cb = (key >> 8) & 255;
+      const unsigned lo = __ballot_sync(kFull, lane < nc && bit(X.la[lane], ca) && bit(X.lb[lane], cb));
+      const unsigned hi =
+          __ballot_sync(kFull, lane + 32 < nc && bit(X.la[lane + 32], ca) && bit(X.lb[lane + 32], cb));
+      const unsigned long long m = (unsigned long long)lo | ((unsigned long long)hi << 32);
+      const int a0 = __ldg(aoff + ca), ny = __ldg(aoff + ca + 1) - a0;
+      const int b0 = __ldg(boff + cb), nz = __ldg(boff + cb + 1) - b0;
+      const int nkq = (nz + 3) >> 2, ntask = ny * nkq;
+      // outer product over the live splits: M[j][k] = max_s A_s[Y_j] + B_s[Z_k]
+      for (int t = lane; t < ntask; t += 32) {
+        const int j = t / nkq, k0 = (t - j * nkq) * 4;
+        const int ai = __ldg(amem + a0 + j);
+        int bi[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) bi[q] = k0 + q < nz ? __ldg(bmem + b0 + k0 + q) : -1;
+        float acc[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = Sr<S>::zero();
+        for (unsigned long long mm = m; mm; mm &= mm - 1) {
+          const int s = __ffsll(mm) - 1;
+          const float* A = X.aptr[c0 + s];
+          const float* B = X.bptr[c0 + s];
+          const float a = __ldg(A + ai);
+          if (S == SEMI_VITERBI) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (bi[q] >= 0) acc[q] = fmaxf(acc[q], a + __ldg(B + bi[q]));
+          } else {
+            const float as = a * X.scl[c0 + s];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (bi[q] >= 0) acc[q] = fmaf(as, __ldg(B + bi[q]), acc[q]);
+          }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+          if (bi[q] >= 0) Mw[j * nz + k0 + q] = acc[q];
+      }
+      __syncwarp();
+      if (lane == 0) work += (unsigned long long)__popcll(m) * ny * nz;
+      // every rule of the pair's gated-in blocks: M[j][k] (x) w into its target
+      const int bk1 = __ldg(J.pair_blk + p + 1);
+      for (int bk = __ldg(J.pair_blk + p); bk < bk1; ++bk) {
+        if (gated && !gate_hit(J, __ldg(J.blk_seg + bk), ms, L.gate_merged, X.gate)) continue;
+        const int r0 = __ldg(J.blk_ptr + bk), r1 = __ldg(J.blk_ptr + bk + 1);
+        const int per = (r1 - r0 + 31) >> 5;
+        const int rs = r0 + lane * per, re = min(r1, rs + per);
+        int cur = -1;
+        float run = Sr<S>::zero();
+        for (int r = rs; r < re; ++r) {
+          const int2 R = __ldg(J.pair_rules + r);
+          const int j = R.x & 255, k = (R.x >> 8) & 255, t = (int)((unsigned)R.x >> 16);
+          const float w = __int_as_float(R.y);
+          const float v = S == SEMI_VITERBI ? Mw[j * nz + k] + w : Mw[j * nz + k] * w;
+          if (t != cur) {
+            if (cur >= 0) flush_run<S>(P, cur, run, corner);
+            cur = t;
+            run = v;
+          } else {
+            run = Sr<S>::add(run, v);
+          }
+        }
+        if (cur >= 0) flush_run<S>(P, cur, run, corner);
+        if (lane == 0) work += (unsigned long long)(r1 - r0);
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+  }
+  if (lane == 0 && (work | corner)) {
+    atomicAdd(&X.work, work);
+    atomicAdd(&X.corner, corner);
+  }
+}
+
+template <int S, int MODE>
+__device__ __forceinline__ void gather(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
+                                       int chunk, CellCtx& X) {
+  if (MODE == 2 && S != SEMI_LOGSUM) gather_pairs<S>(J, L, gated, P, sm, X);
+  else gather_targets<S>(J, L, gated, P, sm.stA, sm.stB, chunk, X);
+}
+
+// Liveness bitset of a shared-memory row (n_valid symbols projected by proj).
+template <int S>
+__device__ void live_bits(const float* row, int n_valid, const int* proj, int ms, CellCtx& X, int* dst) {
+  if (threadIdx.x < kMaxMask) X.words[threadIdx.x] = 0u;
+  __syncthreads();
+  unsigned w[kMaxMask];
+#pragma unroll
+  for (int i = 0; i < kMaxMask; ++i) w[i] = 0u;
+  for (int k = threadIdx.x; k < n_valid; k += blockDim.x) {
+    if (Sr<S>::live(row[k])) {
+      const int c = __ldg(proj + k);
+#pragma unroll
+      for (int i = 0; i < kMaxMask; ++i)
+        if ((c >> 5) == i) w[i] |= 1u << (c & 31);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kMaxMask; ++i) {
+    const unsigned v = __reduce_or_sync(kFull, w[i]);
+    if ((threadIdx.x & 31) == 0 && v) atomicOr(&X.words[i], v);
+  }
+  __syncthreads();
+  if (dst && threadIdx.x < ms) dst[threadIdx.x] = (int)X.words[threadIdx.x];
+}
+
+template <int S>
+__device__ void unary_into(const DevUJob& U, const float* src, float* dst, int cs, bool allowed, float scale) {
+  for (int k = threadIdx.x; k < cs; k += blockDim.x) dst[k] = Sr<S>::zero();
+  if (!allowed) return;
+  for (int t = threadIdx.x; t < U.n_tgt; t += blockDim.x) {
+    const int r0 = __ldg(U.rowptr + t), r1 = __ldg(U.rowptr + t + 1);
+    if (r0 == r1) continue;
+    float acc = Sr<S>::zero();
+    for (int r = r0; r < r1; ++r) {
+      const int2 rr = __ldg(U.rules + r);
+      acc = Sr<S>::mad(acc, src[rr.x], __int_as_float(rr.y));
+    }
+    if (S == SEMI_REAL) acc *= scale;
+    dst[t] = acc;
+  }
+}
+
+__device__ __forceinline__ void store_cell(float* dst, const float* src, int cs) {
+  const int n4 = cs >> 2;
+  for (int k = threadIdx.x; k < n4; k += blockDim.x)
+    reinterpret_cast<float4*>(dst)[k] = reinterpret_cast<const float4*>(src)[k];
+}
+
+__device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
+  if (threadIdx.x == 0) {
+    if (X.work && C.work) atomicAdd(C.work, X.work);
+    if (X.corner && C.corner) atomicAdd(C.corner, X.corner);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Inside pass for one span length (span 1: the unary layer over lexicon cells).
+template <int S, int MODE>
+__global__ void __launch_bounds__(256) k_inside_span(DevLevel L, DevBatch B, DevMask M, int span, float* inside,
+                                                     DevLive V, Counters C, int chunk) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ CellCtx X;
+  const int cs = L.cell_size, ms = L.mask_size;
+  const Smem sm = carve(smem, L, chunk);
+  float* P = sm.P;
+  float* Q = sm.Q;
+  const SentCell sc = span_cell(B, span, blockIdx.x);
+  const int s = sc.s, b = sc.b, e = b + span, n = B.len[s];
+  const long long off = B.cell_off[s], toff = off + tri(n);
+  const long long pbot = off + chart_index(b, e, n), ptop = toff + chart_index(b, e, n);
+  if (threadIdx.x == 0) {
+    X.flag0 = span == 1 ? 1 : mask_any(M, pbot);
+    X.flag1 = mask_any(M, ptop);
+    X.work = 0;
+    X.corner = 0;
+    if (M.bits)
+      for (int i = 0; i < ms; ++i) X.gate[i] = M.bits[pbot * ms + i];
+  }
+  for (int k = threadIdx.x; k < cs; k += blockDim.x) P[k] = Sr<S>::zero();
+  __syncthreads();
+  const bool gated = M.bits != nullptr;
+  const float ps = S == SEMI_REAL ? scale_of(M.iscale, pbot) : 0.f;
+  auto BOT = [&](int x, int y) { return off + chart_index(x, y, n); };
+  auto TOP = [&](int x, int y) { return toff + chart_index(x, y, n); };
+  auto split = [&](long long lc, long long rc) {
+    if (mask_any(M, lc) && mask_any(M, rc))
+      add_split<S>(X, inside + lc * cs, inside + rc * cs, V.in + lc * ms, V.in + rc * ms, scale_of(M.iscale, lc),
+                   scale_of(M.iscale, rc), ps);
+  };
+  if (span == 1) {
+    for (int k = threadIdx.x; k < cs; k += blockDim.x) P[k] = inside[pbot * cs + k];
+  } else if (X.flag0) {
+    for (int job = 0; job < 4; ++job) {
+      const int jid = job == 0 ? IN_TT : job == 1 ? IN_NT : job == 2 ? IN_TN : IN_NN;
+      if (jid == IN_TT && span != 2) continue;
+      if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
+      if (threadIdx.x == 0) {
+        X.nsp = 0;
+        if (jid == IN_NT) split(TOP(b, e - 1), BOT(e - 1, e));
+        else if (jid == IN_TN) split(BOT(b, b + 1), TOP(b + 1, e));
+        else if (jid == IN_TT) split(BOT(b, b + 1), BOT(b + 1, e));
+        else
+          for (int sp = b + 1; sp < e; ++sp) split(TOP(b, sp), TOP(sp, e));
+      }
+      __syncthreads();
+      gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
+    }
+  }
+  __syncthreads();
+  if (span >= 2) {
+    store_cell(inside + pbot * cs, P, cs);
+    live_bits<S>(P, L.n_nt, L.nt_coarse, ms, X, V.in + pbot * ms);
+  }
+  // unary layer: top cell (whole row replaced, CLParser.scala:721-727)
+  const float us = S == SEMI_REAL ? __expf(-scale_of(M.iscale, ptop) + scale_of(M.iscale, pbot)) : 1.f;
+  unary_into<S>(L.ujobs[span == 1 ? IN_TU : IN_NU], P, Q, cs, X.flag1 != 0, us);
+  __syncthreads();
+  store_cell(inside + ptop * cs, Q, cs);
+  live_bits<S>(Q, L.n_nt, L.nt_coarse, ms, X, V.in + ptop * ms);
+  flush_counters(X, C);
+}
+
+// ---------------------------------------------------------------------------
+// Outside pass for one span length: outside-top of each cell gathered from its
+// parents, then the unary layer to outside-bot (and, at span 1, the
+// terminal-child binaries that the reference runs after its span loop).
+template <int S, int MODE>
+__global__ void __launch_bounds__(256) k_outside_span(DevLevel L, DevBatch B, DevMask M, int span,
+                                                      const float* inside, float* outside, DevLive V, Counters C,
+                                                      int chunk) {
+  extern __shared__ __align__(16) float smem[];
+  __shared__ CellCtx X;
+  const int cs = L.cell_size, ms = L.mask_size;
+  const Smem sm = carve(smem, L, chunk);
+  float* P = sm.P;
+  float* Q = sm.Q;
+  const SentCell sc = span_cell(B, span, blockIdx.x);
+  const int s = sc.s, b = sc.b, e = b + span, n = B.len[s];
+  const long long off = B.cell_off[s], toff = off + tri(n);
+  const long long cbot = off + chart_index(b, e, n), ctop = toff + chart_index(b, e, n);
+  auto BOT = [&](int x, int y) { return off + chart_index(x, y, n); };
+  auto TOP = [&](int x, int y) { return toff + chart_index(x, y, n); };
+  const bool gated = M.bits != nullptr;
+  if (threadIdx.x == 0) {
+    X.flag0 = mask_any(M, ctop);
+    X.flag1 = mask_any(M, cbot);
+    X.work = 0;
+    X.corner = 0;
+    if (M.bits)
+      for (int i = 0; i < ms; ++i) X.gate[i] = M.bits[ctop * ms + i];
+  }
+  for (int k = threadIdx.x; k < cs; k += blockDim.x) P[k] = Sr<S>::zero();
+  __syncthreads();
+  const float* IS = M.iscale;
+  const float* OS = M.oscale;
+  // operand helpers: (outside parent, inside sibling) or (inside sibling, outside parent)
+  float ps = 0.f;
+  auto split_oi = [&](long long oc, long long ic) {
+    if (mask_any(M, oc) && mask_any(M, ic))
+      add_split<S>(X, outside + oc * cs, inside + ic * cs, V.out + oc * ms, V.in + ic * ms, scale_of(OS, oc),
+                   scale_of(IS, ic), ps);
+  };
+  auto split_io = [&](long long ic, long long oc) {
+    if (mask_any(M, ic) && mask_any(M, oc))
+      add_split<S>(X, inside + ic * cs, outside + oc * cs, V.in + ic * ms, V.out + oc * ms, scale_of(IS, ic),
+                   scale_of(OS, oc), ps);
+  };
+  if (span == n) {
+    if (threadIdx.x == 0) P[L.root] = Sr<S>::one();  // setRootScores
+  } else if (X.flag0) {
+    ps = S == SEMI_REAL ? scale_of(OS, ctop) : 0.f;
+    for (int job = 0; job < 4; ++job) {
+      const int jid = job == 0 ? OUT_R_TN : job == 1 ? OUT_L_NT : job == 2 ? OUT_L_NN : OUT_R_NN;
+      if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
+      if (threadIdx.x == 0) {
+        X.nsp = 0;
+        if (jid == OUT_R_TN) {
+          if (b >= 1) split_io(BOT(b - 1, b), BOT(b - 1, e));
+        } else if (jid == OUT_L_NT) {
+          if (e + 1 <= n) split_oi(BOT(b, e + 1), BOT(e, e + 1));
+        } else if (jid == OUT_L_NN) {
+          for (int sp = e + 1; sp <= n; ++sp) split_oi(BOT(b, sp), TOP(e, sp));
+        } else {
+          for (int sp = 0; sp < b; ++sp) split_io(TOP(sp, b), BOT(sp, e));
+        }
+      }
+      __syncthreads();
+      gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
+    }
+  }
+  __syncthreads();
+  store_cell(outside + ctop * cs, P, cs);
+  live_bits<S>(P, L.n_nt, L.nt_coarse, ms, X, V.out ? V.out + ctop * ms : nullptr);
+  // unary layer: outside-bot from outside-top.  With a batch of one-word
+  // sentences only, the reference's first unary call (at span == maxLength)
+  // uses the nonterminal unaries and its span loop never runs.
+  const bool use_tu = span == 1 && B.max_len > 1;
+  const float us = S == SEMI_REAL ? __expf(-scale_of(OS, cbot) + scale_of(OS, ctop)) : 1.f;
+  unary_into<S>(L.ujobs[use_tu ? OUT_TU : OUT_NU], P, Q, cs, X.flag0 != 0, us);
+  __syncthreads();
+  if (span == 1 && X.flag1) {
+    // terminal-child buckets, gated by the bot cell's mask (CLParser.scala:345-355)
+    if (threadIdx.x == 0 && M.bits)
+      for (int i = 0; i < ms; ++i) X.gate[i] = M.bits[cbot * ms + i];
+    ps = S == SEMI_REAL ? scale_of(OS, cbot) : 0.f;
+    for (int job = 0; job < 4; ++job) {
+      const int jid = job == 0 ? OUT_L_TT : job == 1 ? OUT_R_NT : job == 2 ? OUT_L_TN : OUT_R_TT;
+      if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
+      if (threadIdx.x == 0) {
+        X.nsp = 0;
+        if (jid == OUT_L_TT) {
+          if (b + 2 <= n) split_oi(BOT(b, b + 2), BOT(b + 1, b + 2));
+        } else if (jid == OUT_R_NT) {
+          for (int sp = 0; sp < b; ++sp) split_io(TOP(sp, b), BOT(sp, b + 1));
+        } else if (jid == OUT_L_TN) {
+          for (int sp = b + 2; sp <= n; ++sp) split_oi(BOT(b, sp), TOP(b + 1, sp));
+        } else {
+          if (b >= 1) split_io(BOT(b - 1, b), BOT(b - 1, b + 1));
+        }
+      }
+      __syncthreads();
+      gather<S, MODE>(L.jobs[jid], L, gated, Q, sm, chunk, X);
+    }
+  }
+  __syncthreads();
+  store_cell(outside + cbot * cs, Q, cs);
+  const bool term = span == 1 && use_tu;
+  live_bits<S>(Q, term ? L.n_t : L.n_nt, term ? L.t_coarse : L.nt_coarse, ms, X,
+               V.out ? V.out + cbot * ms : nullptr);
+  flush_counters(X, C);
+}
+
+// ---------------------------------------------------------------------------
+// Lexicon (CLParser.scala:426-467): one warp per token writes its bot span-1
+// cell: the semiring zero except the word's allowed preterminals.
+template <int S>
+__global__ void k_lexicon(DevLevel L, DevBatch B, DevMask M, float* inside, double* part_scale, DevLive V,
+                          int* status) {
+  const long long tok = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (tok >= B.num_tokens) return;
+  int lo = 0, hi = B.nsent;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (B.word_off[mid] <= tok) lo = mid; else hi = mid;
+  }
+  const int s = lo, pos = (int)(tok - B.word_off[s]);
+  const int cs = L.cell_size, ms = L.mask_size;
+  const long long cell = B.cell_off[s] + pos;  // chartIndex(pos, pos + 1) == pos
+  float* row = inside + cell * cs;
+  for (int k = lane; k < cs; k += 32) row[k] = Sr<S>::zero();
+  __syncwarp();
+  const int w = B.words[tok];
+  unsigned bits[kMaxMask];
+#pragma unroll
+  for (int i = 0; i < kMaxMask; ++i) bits[i] = 0u;
+  if (w < 0 || w >= L.n_words) {
+    if (lane == 0 && status) status[s] = 4;  // PUCK_ERR_OOV
+  } else {
+    const long long x0 = L.lex_off[w], x1 = L.lex_off[w + 1];
+    for (long long x = x0 + lane; x < x1; x += 32) {
+      const int c = L.t_coarse[L.lex_term[x]];
+#pragma unroll
+      for (int i = 0; i < kMaxMask; ++i)
+        if ((c >> 5) == i) bits[i] |= 1u << (c & 31);
+    }
+    if (S == SEMI_REAL) {
+      const float my_scale = __expf(-scale_of(M.iscale, cell));
+      float total = 0.f;
+      for (long long x = x0 + lane; x < x1; x += 32) {
+        const float v = __expf(L.lex_score[x]) * my_scale;
+        row[L.lex_term[x]] = v;
+        total += v;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(kFull, total, o);
+      __syncwarp();
+      const float half = total / 2.f;
+      for (long long x = x0 + lane; x < x1; x += 32) row[L.lex_term[x]] /= half;
+      if (lane == 0) atomicAdd(part_scale + s, log((double)half));
+    } else {
+      for (long long x = x0 + lane; x < x1; x += 32) row[L.lex_term[x]] = L.lex_score[x];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < kMaxMask; ++i) {
+    const unsigned v = __reduce_or_sync(kFull, bits[i]);
+    if (lane == 0 && i < ms) V.in[cell * ms + i] = (int)v;
+  }
+}
+
+template <class K>
+void set_smem(K kernel, size_t bytes) {
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+}  // namespace
+
+size_t pass_smem_bytes(const DevLevel& L, int chunk) {
+  const size_t cs = L.cell_size;
+  if (L.mode == 2)
+    return (2 * cs + (size_t)(kThreads / 32) * L.max_mtile) * sizeof(float) +
+           (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int);
+  return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);
+}
+
+// Splits staged per chunk by the target-major mode: as many as fit with two
+// CTAs per SM.
+int pick_split_chunk(int cell_size, int max_len) {
+  const int static_bytes = (int)sizeof(CellCtx);
+  const int budget = (112 * 1024 - static_bytes) / 4;
+  int chunk = (budget - 2 * cell_size) / (2 * cell_size);
+  chunk = chunk < 2 ? 2 : chunk;
+  chunk = chunk > kMaxSplitChunk ? kMaxSplitChunk : chunk;
+  if (max_len > 1 && chunk > max_len) chunk = max_len;
+  return chunk;
+}
+
+cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevMask& M, float* inside,
+                           double* part_scale, DevLive V, Counters C, cudaStream_t st) {
+  const long long warps = B.num_tokens;
+  const int blocks = (int)((warps * 32 + 127) / 128);
+  if (blocks == 0) return cudaSuccess;
+  switch (L.semiring) {
+    case SEMI_VITERBI: k_lexicon<SEMI_VITERBI><<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, V, C.status); break;
+    case SEMI_REAL: k_lexicon<SEMI_REAL><<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, V, C.status); break;
+    default: k_lexicon<SEMI_LOGSUM><<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, V, C.status); break;
+  }
+  return cudaGetLastError();
+}
+
+namespace {
+
+template <int S, int MODE>
+cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
+                        const float* inside_c, float* inside, float* outside, DevLive V, Counters C, cudaStream_t st) {
+  const int chunk = pick_split_chunk(L.cell_size, B.max_len);
+  const size_t smem = pass_smem_bytes(L, chunk);
+  if (inside_pass) {
+    set_smem(k_inside_span<S, MODE>, smem);
+    k_inside_span<S, MODE><<<ncells, kThreads, smem, st>>>(L, B, M, span, inside, V, C, chunk);
+  } else {
+    set_smem(k_outside_span<S, MODE>, smem);
+    k_outside_span<S, MODE><<<ncells, kThreads, smem, st>>>(L, B, M, span, inside_c, outside, V, C, chunk);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_any(bool inside_pass, const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
+                       const float* inside_c, float* inside, float* outside, DevLive V, Counters C, cudaStream_t st) {
+  if (ncells == 0) return cudaSuccess;
+  const bool pairs = L.mode == 2;
+  switch (L.semiring) {
+    case SEMI_VITERBI:
+      return pairs ? launch_pass<SEMI_VITERBI, 2>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st)
+                   : launch_pass<SEMI_VITERBI, 0>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st);
+    case SEMI_REAL:
+      return pairs ? launch_pass<SEMI_REAL, 2>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st)
+                   : launch_pass<SEMI_REAL, 0>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st);
+    default:
+      return launch_pass<SEMI_LOGSUM, 0>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
+                               float* inside, DevLive V, Counters C, cudaStream_t st) {
+  return launch_any(true, L, B, M, span, ncells, inside, inside, nullptr, V, C, st);
+}
+
+cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
+                                const float* inside, float* outside, DevLive V, Counters C, cudaStream_t st) {
+  return launch_any(false, L, B, M, span, ncells, inside, nullptr, outside, V, C, st);
+}
+
+}  // namespace puck

@@ -15,6 +15,7 @@ enum JobId { IN_NN, IN_NT, IN_TN, IN_TT, OUT_L_NN, OUT_R_NN, OUT_L_NT, OUT_R_NT,
 enum UJobId { IN_NU, IN_TU, OUT_NU, OUT_TU, NUJOBS };
 
 constexpr int kMaxMask = 8;        // up to 256 coarse symbols
+constexpr int kMaxCoarse = 256;
 constexpr int kMaxSplitChunk = 32;  // splits staged in shared memory at once
 constexpr int kMaxLen = 256;        // longest sentence a parser accepts
 
@@ -27,6 +28,18 @@ struct DevJob {
   const int2* rules;    // [rowptr[n_tgt]]
   const int* tgt_seg;   // [n_tgt] segment of the target's rules, -1 if none
   const int* seg_bits;  // [nseg * mask_size] coarse-parent bitset of each segment
+  // pair-factored layout (level mode 2): rules grouped by the coarse
+  // projection (ca, cb) of their operands ("pairs"), then by segment
+  // ("blocks"), then by target; rules {j | k << 8 | target << 16, bits(w)}
+  // with j, k the operands' positions among their coarse symbol's members.
+  int npair;
+  int a_is_t, b_is_t;
+  const int* pair_key;    // [npair] ca | cb << 8
+  const int* pair_gate;   // [npair * mask_size] OR of the pair's segment bits
+  const int* pair_blk;    // [npair + 1] block range
+  const int* blk_seg;     // [nblk]
+  const int* blk_ptr;     // [nblk + 1] rule range
+  const int2* pair_rules;
 };
 
 struct DevUJob {
@@ -38,6 +51,13 @@ struct DevUJob {
 struct DevLevel {
   int semiring, n_nt, n_t, cell_size, mask_size, n_coarse, root, num_syms, n_words;
   int gate_merged;  // non-final level of a cascade: every target gated by segment 0's bits
+  int mode;         // 0: target-major rule scans, 2: pair-factored
+  int max_npair;    // largest pair count of any job (shared-memory list size)
+  int max_mtile;    // largest ny * nz of any pair (per-warp outer-product tile)
+  const int* nt_mem_off;  // [n_coarse + 1] coarse -> nonterminal members
+  const int* nt_mem;
+  const int* t_mem_off;   // [n_coarse + 1] coarse -> terminal members
+  const int* t_mem;
   const int* nt_coarse;
   const int* t_coarse;
   DevJob jobs[NJOBS];
@@ -87,12 +107,19 @@ struct Counters {
   int* status;                  // per-sentence status codes
 };
 
+// Liveness bitsets of a chart: per cell, bit c set iff some symbol that
+// projects onto coarse symbol c is not the semiring zero.
+struct DevLive {
+  int* in;    // [num_cells * mask_size] inside chart
+  int* out;   // [num_cells * mask_size] outside chart (may be null)
+};
+
 cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevMask& M, float* inside,
-                           double* part_scale, Counters C, cudaStream_t st);
+                           double* part_scale, DevLive V, Counters C, cudaStream_t st);
 cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                               float* inside, Counters C, cudaStream_t st);
+                               float* inside, DevLive V, Counters C, cudaStream_t st);
 cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                                const float* inside, float* outside, Counters C, cudaStream_t st);
+                                const float* inside, float* outside, DevLive V, Counters C, cudaStream_t st);
 cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
                          float thresh, int* masks_out, cudaStream_t st);
 cudaError_t launch_scaling(int cell_size, long long num_cells, const float* chart, float* out, cudaStream_t st);
@@ -105,7 +132,7 @@ cudaError_t launch_mbr_decode(const DevBatch& B, const DevMask& M, int scaling, 
 cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevMask& M, const float* inside,
                                const double* part_scale, float* log_z, cudaStream_t st);
 
-size_t inside_smem_bytes(int cell_size, int chunk);
+size_t pass_smem_bytes(const DevLevel& L, int chunk);
 int pick_split_chunk(int cell_size, int max_len);
 
 }  // namespace puck

@@ -14,6 +14,7 @@
 #include "../../include/puck_gpu.h"
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -183,6 +184,40 @@ void validate_level(const HostLevel& L) {
     const int64_t nbits = need(n + "/seg_bits", "i4", -1);
     if (L.mask_size <= 0 || nbits % L.mask_size) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad seg_bits for " + n};
     need(n + "/tgt_seg", "i4", ntgt);
+    need(n + "/pair_mode", "i4", 1);
+    {
+      const int64_t npk = need(n + "/pair_key", "i4", -1);
+      need(n + "/pair_gate", "i4", npk * L.mask_size);
+      const int64_t npb = need(n + "/pair_blk", "i4", npk + 1);
+      const int64_t nbs = need(n + "/blk_seg", "i4", -1);
+      const int64_t nbp = need(n + "/blk_ptr", "i4", nbs + 1);
+      const int64_t npr = need(n + "/pair_rule", "i4", nab);
+      need(n + "/pair_w", "f4", nab);
+      const int* pk = L.get<int>(n + "/pair_key", "i4", nullptr);
+      const int* pb = L.get<int>(n + "/pair_blk", "i4", nullptr);
+      const int* bs = L.get<int>(n + "/blk_seg", "i4", nullptr);
+      const int* bp = L.get<int>(n + "/blk_ptr", "i4", nullptr);
+      const int* pr = L.get<int>(n + "/pair_rule", "i4", nullptr);
+      const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+      const int* bo = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+      if (pb[0] != 0 || pb[npb - 1] != nbs || bp[0] != 0 || bp[nbp - 1] != npr)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad pair tables for " + n};
+      for (int64_t k = 0; k < npk; ++k) {
+        const int ca = pk[k] & 255, cb = (pk[k] >> 8) & 255;
+        if (ca >= L.n_coarse || cb >= L.n_coarse || pb[k + 1] < pb[k])
+          throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad pair key for " + n};
+        const int ny = ao[ca + 1] - ao[ca], nz = bo[cb + 1] - bo[cb];
+        if (ny > 255 || nz > 255) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "coarse symbol with more than 255 members"};
+        for (int b = pb[k]; b < pb[k + 1]; ++b) {
+          if (bs[b] < 0 || bs[b] >= nbits / std::max(1, L.mask_size) || bp[b + 1] < bp[b])
+            throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad block for " + n};
+          for (int r = bp[b]; r < bp[b + 1]; ++r) {
+            const int jj = pr[r] & 255, kk = (pr[r] >> 8) & 255, tt = (int)((unsigned)pr[r] >> 16);
+            if (jj >= ny || kk >= nz || tt >= ntgt) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule out of range in " + n};
+          }
+        }
+      }
+    }
     int64_t c = 0;
     const int* ts = L.get<int>(n + "/tgt_seg", "i4", &c);
     for (int64_t k = 0; k < c; ++k)
@@ -198,6 +233,12 @@ void validate_level(const HostLevel& L) {
     need(n + "/w", "f4", ns);
     range(n + "/src", us[j] ? L.n_t : L.n_nt);
   }
+  need("nt_mem_off", "i4", L.n_coarse + 1);
+  need("t_mem_off", "i4", L.n_coarse + 1);
+  need("nt_mem", "i4", L.n_nt);
+  need("t_mem", "i4", L.n_t);
+  range("nt_mem", L.n_nt);
+  range("t_mem", L.n_t);
   const int64_t nlo = need("lex_off", "i8", L.n_words + 1);
   const long long* lo = L.get<long long>("lex_off", "i8", nullptr);
   need("lex_term", "i4", lo[nlo - 1]);
@@ -242,7 +283,8 @@ void load_grammar(puck_grammar* g, const std::string& path) {
     L.n_coarse = geti("n_coarse");
     L.root = geti("root");
     L.n_words = geti("n_words");
-    if (L.mask_size > puck::kMaxMask) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "too many coarse symbols"};
+    if (L.mask_size > puck::kMaxMask || L.n_coarse > puck::kMaxCoarse)
+      throw PuckError{PUCK_ERR_BAD_GRAMMAR, "too many coarse symbols"};
     if (L.cell_size % 32 != 0 || L.cell_size < std::max(L.n_nt, L.n_t))
       throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad cell size"};
     if (std::max(L.n_nt, L.n_t) > 65535) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "more than 65535 symbols"};
@@ -352,6 +394,41 @@ void build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.tgt_seg = up<int>(D, L, n + "/tgt_seg", "i4");
     J.seg_bits = up<int>(D, L, n + "/seg_bits", "i4", &nseg);
     J.nseg = (int)(nseg / std::max(1, L.mask_size));
+    static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
+    static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
+    int64_t npk = 0, nr = 0;
+    const int* pk = L.get<int>(n + "/pair_key", "i4", &npk);
+    const int* pr = L.get<int>(n + "/pair_rule", "i4", &nr);
+    const float* pw = L.get<float>(n + "/pair_w", "f4", nullptr);
+    std::vector<int2> rr(nr);
+    for (int64_t k = 0; k < nr; ++k) {
+      rr[k].x = pr[k];
+      std::memcpy(&rr[k].y, &pw[k], 4);
+    }
+    J.npair = (int)npk;
+    J.a_is_t = a_t[j];
+    J.b_is_t = b_t[j];
+    J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
+    J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
+    J.pair_blk = up<int>(D, L, n + "/pair_blk", "i4");
+    J.blk_seg = up<int>(D, L, n + "/blk_seg", "i4");
+    J.blk_ptr = up<int>(D, L, n + "/blk_ptr", "i4");
+    J.pair_rules = reinterpret_cast<const int2*>(D.upload(rr.data(), rr.size() * sizeof(int2)));
+    d.max_npair = std::max(d.max_npair, J.npair);
+    const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+    const int* bo = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+    for (int64_t k = 0; k < npk; ++k) {
+      const int ca = pk[k] & 255, cb = (pk[k] >> 8) & 255;
+      d.max_mtile = std::max(d.max_mtile, (ao[ca + 1] - ao[ca]) * (bo[cb + 1] - bo[cb]));
+    }
+  }
+  {
+    const int* nn_mode = L.get<int>("in_NN/pair_mode", "i4", nullptr);
+    d.mode = (nn_mode[0] == 2 && L.semiring != puck::SEMI_LOGSUM) ? 2 : 0;
+    d.nt_mem_off = up<int>(D, L, "nt_mem_off", "i4");
+    d.nt_mem = up<int>(D, L, "nt_mem", "i4");
+    d.t_mem_off = up<int>(D, L, "t_mem_off", "i4");
+    d.t_mem = up<int>(D, L, "t_mem", "i4");
   }
   for (int j = 0; j < puck::NUJOBS; ++j) {
     const std::string n = kUJobNames[j];
@@ -384,7 +461,7 @@ long long tri(int n) { return (long long)n * (n + 1) / 2; }
 enum Mode { MODE_PARSE = 0, MODE_PARTITIONS = 1, MODE_INSIDE_OUTSIDE = 2 };
 
 struct LevelBufs {
-  DevBuf inside, outside, masks, iscale, oscale, part, decode;
+  DevBuf inside, outside, masks, iscale, oscale, part, decode, live_in, live_out;
 };
 
 }  // namespace
@@ -402,7 +479,10 @@ struct puck_parser {
   int last_batches = 0;
   puck_stats stats{};
   int64_t budget_bytes = 0;
-  cudaEvent_t ev[8];
+  cudaEvent_t ev_batch[2] = {nullptr, nullptr};
+  std::vector<std::array<cudaEvent_t, 5>> ev_level;   // per level: in0, in1, out1, mask1, dec1
+  std::vector<std::array<double, 4>> pass_ms;
+  std::vector<std::array<int64_t, 4>> pass_launches;
 };
 
 namespace {
@@ -415,7 +495,7 @@ int64_t bytes_per_cell(const puck_parser* P, Mode mode) {
     const bool last = l == nl - 1;
     const bool need_out = !last || mode == MODE_INSIDE_OUTSIDE || (mode == MODE_PARSE && L.semiring != 0 &&
                                                                     P->opt.decode != PUCK_DECODE_VITERBI);
-    b += (int64_t)L.cell_size * 4 * (need_out ? 2 : 1);
+    b += (int64_t)(L.cell_size + L.mask_size) * 4 * (need_out ? 2 : 1);  // chart + liveness
     if (!last) b += (int64_t)L.mask_size * 4 + 8;
     else b += 8;
   }
@@ -469,6 +549,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   auto h2d = [&](DevBuf& b, const void* src, size_t bytes) {
     b.ensure(std::max<size_t>(bytes, 16));
     if (bytes) CUDA_TRY(cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, st));
+    P->stats.h2d_bytes += (int64_t)bytes;
   };
   h2d(P->b_len, len.data(), ns * sizeof(int));
   h2d(P->b_cell_off, cell_off.data(), (ns + 1) * sizeof(long long));
@@ -500,21 +581,10 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   puck::Counters C{P->b_counters.as<unsigned long long>(), P->b_counters.as<unsigned long long>() + 1,
                    P->b_status.as<int>()};
 
-  const bool prof = P->opt.profile != 0;
-  auto mark = [&](int i) {
-    if (prof) CUDA_TRY(cudaEventRecord(P->ev[i], st));
-  };
-  double ms_in = 0, ms_out = 0, ms_mask = 0, ms_dec = 0;
-  auto elapsed = [&](int a, int b) {
-    if (!prof) return 0.0;
-    CUDA_TRY(cudaEventSynchronize(P->ev[b]));
-    float ms = 0;
-    CUDA_TRY(cudaEventElapsedTime(&ms, P->ev[a], P->ev[b]));
-    return (double)ms;
-  };
-
+  auto rec = [&](cudaEvent_t e) { CUDA_TRY(cudaEventRecord(e, st)); };
+  std::vector<std::array<int64_t, 4>> launches_l(nl, std::array<int64_t, 4>{0, 0, 0, 0});
+  rec(P->ev_batch[0]);
   puck::DevMask M{nullptr, 0, nullptr, nullptr};
-  int64_t launches = 0;
   for (int l = 0; l < nl; ++l) {
     const puck::DevLevel& D = P->levels[l]->d;
     const HostLevel& HL = P->g->levels[l];
@@ -528,42 +598,45 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     CUDA_TRY(cudaMemsetAsync(lb.part.p, 0, ns * sizeof(double), st));
     float* inside = lb.inside.as<float>();
     float* outside = need_out ? lb.outside.as<float>() : nullptr;
+    lb.live_in.ensure(num_cells * D.mask_size * sizeof(int));
+    if (need_out) lb.live_out.ensure(num_cells * D.mask_size * sizeof(int));
+    const puck::DevLive V{lb.live_in.as<int>(), need_out ? lb.live_out.as<int>() : nullptr};
     puck::DevMask MM = M;
     if (D.semiring != puck::SEMI_REAL) { MM.iscale = nullptr; MM.oscale = nullptr; }
-    mark(0);
-    CUDA_TRY(puck::launch_lexicon(D, B, MM, inside, lb.part.as<double>(), C, st));
-    ++launches;
+    auto& EV = P->ev_level[l];
+    auto& LC = launches_l[l];
+    rec(EV[0]);
+    CUDA_TRY(puck::launch_lexicon(D, B, MM, inside, lb.part.as<double>(), V, C, st));
+    ++LC[0];
     for (int span = 1; span <= max_len; ++span) {
-      CUDA_TRY(puck::launch_inside_span(D, B, MM, span, span_cells[span], inside, C, st));
-      ++launches;
+      CUDA_TRY(puck::launch_inside_span(D, B, MM, span, span_cells[span], inside, V, C, st));
+      ++LC[0];
     }
-    mark(1);
+    rec(EV[1]);
     if (need_out) {
       for (int span = max_len; span >= 1; --span) {
-        CUDA_TRY(puck::launch_outside_span(D, B, MM, span, span_cells[span], inside, outside, C, st));
-        ++launches;
+        CUDA_TRY(puck::launch_outside_span(D, B, MM, span, span_cells[span], inside, outside, V, C, st));
+        ++LC[1];
       }
     }
-    mark(2);
-    ms_in += elapsed(0, 1);
-    ms_out += elapsed(1, 2);
+    rec(EV[2]);
     if (!last) {
       lb.masks.ensure(num_cells * D.mask_size * sizeof(int));
       CUDA_TRY(puck::launch_masks(D, B, inside, outside, P->opt.prune_threshold, lb.masks.as<int>(), st));
-      ++launches;
+      ++LC[2];
       lb.iscale.ensure(num_cells * sizeof(float));
       lb.oscale.ensure(num_cells * sizeof(float));
       const bool next_real = P->g->levels[l + 1].semiring == puck::SEMI_REAL;
       if (next_real) {
         CUDA_TRY(puck::launch_scaling(D.cell_size, num_cells, inside, lb.iscale.as<float>(), st));
         CUDA_TRY(puck::launch_scaling(D.cell_size, num_cells, outside, lb.oscale.as<float>(), st));
-        launches += 2;
+        LC[2] += 2;
       } else {
         CUDA_TRY(cudaMemsetAsync(lb.iscale.p, 0, num_cells * sizeof(float), st));
         CUDA_TRY(cudaMemsetAsync(lb.oscale.p, 0, num_cells * sizeof(float), st));
       }
-      mark(3);
-      ms_mask += elapsed(2, 3);
+      rec(EV[3]);
+      rec(EV[4]);
       M.bits = lb.masks.as<int>();
       M.mask_size = D.mask_size;
       M.iscale = lb.iscale.as<float>();
@@ -571,13 +644,16 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
       continue;
     }
     // last level
-    mark(4);
+    rec(EV[3]);
     if (mode == MODE_PARTITIONS) {
       P->b_logz.ensure(ns * sizeof(float) + 16);
       CUDA_TRY(puck::launch_root_scores(D, B, MM, inside, lb.part.as<double>(), P->b_logz.as<float>(), st));
-      ++launches;
+      ++LC[3];
+      rec(EV[4]);
+      rec(P->ev_batch[1]);
       std::vector<float> lz(ns);
       CUDA_TRY(cudaMemcpyAsync(lz.data(), P->b_logz.p, ns * sizeof(float), cudaMemcpyDeviceToHost, st));
+      P->stats.d2h_bytes += (int64_t)(ns * sizeof(float));
       CUDA_TRY(cudaStreamSynchronize(st));
       for (int i = 0; i < ns; ++i) log_z[plan.sent[i]] = lz[i];
     } else if (mode == MODE_PARSE) {
@@ -588,7 +664,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
         if (D.semiring != puck::SEMI_VITERBI)
           throw PuckError{PUCK_ERR_INVALID_ARG, "Viterbi decoding needs a Viterbi fine level"};
         CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
-        ++launches;
+        ++LC[3];
       } else {
         if (!M.bits) throw PuckError{PUCK_ERR_INVALID_ARG, "Can't use null pruning mask for parse extraction!"};
         if (D.semiring == puck::SEMI_VITERBI)
@@ -600,10 +676,13 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
         CUDA_TRY(puck::launch_mbr_decode(B, M, D.semiring == puck::SEMI_REAL ? 1 : 0, lb.decode.as<float2>(),
                                          P->b_mbr_off.as<long long>(), P->b_scratch.as<float>(),
                                          P->b_nodes.as<puck::DevNode>(), st));
-        launches += 2;
+        LC[3] += 2;
       }
+      rec(EV[4]);
+      rec(P->ev_batch[1]);
       std::vector<puck::DevNode> hn(node_off[ns]);
       CUDA_TRY(cudaMemcpyAsync(hn.data(), P->b_nodes.p, hn.size() * sizeof(puck::DevNode), cudaMemcpyDeviceToHost, st));
+      P->stats.d2h_bytes += (int64_t)(hn.size() * sizeof(puck::DevNode));
       CUDA_TRY(cudaStreamSynchronize(st));
       for (int i = 0; i < ns; ++i) {
         const int s = plan.sent[i];
@@ -611,19 +690,18 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
                     (2 * len[i] - 1) * sizeof(puck_tree_node));
       }
     } else {
-      if (!last || true) {
-        if (D.semiring == puck::SEMI_VITERBI) {
-          P->b_nodes.ensure(node_off[ns] * sizeof(puck::DevNode) + 16);
-          CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
-        } else {
-          lb.decode.ensure(num_cells * sizeof(float2));
-          CUDA_TRY(puck::launch_mbr_cells(D, B, inside, outside, lb.decode.as<float2>(), st));
-        }
-        ++launches;
+      // insideOutside: the decode kernels run, nothing is extracted (CLParser.scala:171-182)
+      if (D.semiring == puck::SEMI_VITERBI) {
+        P->b_nodes.ensure(node_off[ns] * sizeof(puck::DevNode) + 16);
+        CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
+      } else {
+        lb.decode.ensure(num_cells * sizeof(float2));
+        CUDA_TRY(puck::launch_mbr_cells(D, B, inside, outside, lb.decode.as<float2>(), st));
       }
+      ++LC[3];
+      rec(EV[4]);
+      rec(P->ev_batch[1]);
     }
-    mark(5);
-    ms_dec += elapsed(4, 5);
   }
   std::vector<int> status(ns);
   unsigned long long ctr[2] = {0, 0};
@@ -633,10 +711,27 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   if (sent_status)
     for (int i = 0; i < ns; ++i)
       if (status[i]) sent_status[plan.sent[i]] = status[i];
-  P->stats.ms_inside += ms_in;
-  P->stats.ms_outside += ms_out;
-  P->stats.ms_masks += ms_mask;
-  P->stats.ms_decode += ms_dec;
+  auto ms_between = [](cudaEvent_t a, cudaEvent_t b) {
+    float ms = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&ms, a, b));
+    return (double)ms;
+  };
+  int64_t launches = 0;
+  for (int l = 0; l < nl; ++l) {
+    auto& EV = P->ev_level[l];
+    const double t[4] = {ms_between(EV[0], EV[1]), ms_between(EV[1], EV[2]), ms_between(EV[2], EV[3]),
+                         ms_between(EV[3], EV[4])};
+    for (int k = 0; k < 4; ++k) {
+      P->pass_ms[l][k] += t[k];
+      P->pass_launches[l][k] += launches_l[l][k];
+      launches += launches_l[l][k];
+    }
+    P->stats.ms_inside += t[0];
+    P->stats.ms_outside += t[1];
+    P->stats.ms_masks += t[2];
+    P->stats.ms_decode += t[3];
+  }
+  P->stats.ms_device += ms_between(P->ev_batch[0], P->ev_batch[1]);
   P->stats.cells += num_cells;
   P->stats.binary_work += (int64_t)ctr[1];
   P->stats.kernel_launches += launches;
@@ -653,6 +748,8 @@ puck_status run_call(puck_parser* P, Mode mode, const int32_t* word_ids, const i
     CUDA_TRY(cudaSetDevice(P->opt.device));
     const auto t0 = std::chrono::steady_clock::now();
     P->stats = puck_stats{};
+    for (auto& a : P->pass_ms) a = {0, 0, 0, 0};
+    for (auto& a : P->pass_launches) a = {0, 0, 0, 0};
     const int nwords = P->g->levels.back().n_words;
     std::vector<int64_t> node_off(nsent + 1, 0);
     std::vector<int> valid;
@@ -780,8 +877,13 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
     if (P->opt.device < 0 || P->opt.device >= ndev) throw PuckError{PUCK_ERR_INVALID_ARG, "no such CUDA device"};
     CUDA_TRY(cudaSetDevice(P->opt.device));
     CUDA_TRY(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
-    for (auto& e : P->ev) CUDA_TRY(cudaEventCreate(&e));
     const int nl = (int)g->levels.size();
+    for (auto& e : P->ev_batch) CUDA_TRY(cudaEventCreate(&e));
+    P->ev_level.resize(nl);
+    for (auto& a : P->ev_level)
+      for (auto& e : a) CUDA_TRY(cudaEventCreate(&e));
+    P->pass_ms.assign(nl, std::array<double, 4>{0, 0, 0, 0});
+    P->pass_launches.assign(nl, std::array<int64_t, 4>{0, 0, 0, 0});
     for (int l = 0; l < nl; ++l) {
       P->levels.emplace_back(new LevelDev());
       build_level(*P->levels.back(), g->levels[l], l < nl - 1 && nl != 1);
@@ -806,15 +908,18 @@ void puck_parser_destroy(puck_parser* P) {
   cudaSetDevice(P->opt.device);
   for (auto& b : P->bufs) {
     b.inside.release(); b.outside.release(); b.masks.release(); b.iscale.release(); b.oscale.release();
-    b.part.release(); b.decode.release();
+    b.part.release(); b.decode.release(); b.live_in.release(); b.live_out.release();
   }
   for (DevBuf* b : {&P->b_len, &P->b_cell_off, &P->b_word_off, &P->b_words, &P->b_order, &P->b_span_pref,
                     &P->b_span_base, &P->b_span_count, &P->b_node_off, &P->b_mbr_off, &P->b_nodes, &P->b_status,
                     &P->b_logz, &P->b_scratch, &P->b_counters})
     b->release();
   P->levels.clear();
-  for (auto& e : P->ev)
+  for (auto& e : P->ev_batch)
     if (e) cudaEventDestroy(e);
+  for (auto& a : P->ev_level)
+    for (auto& e : a)
+      if (e) cudaEventDestroy(e);
   if (P->stream) cudaStreamDestroy(P->stream);
   delete P;
 }
@@ -877,6 +982,18 @@ puck_status puck_debug_copy(puck_parser* P, int32_t level, int32_t which, void* 
 puck_status puck_parser_stats(const puck_parser* p, puck_stats* out) {
   if (!p || !out) return PUCK_ERR_INVALID_ARG;
   *out = p->stats;
+  return PUCK_OK;
+}
+
+puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[4], int64_t launches[4]) {
+  if (!p || level < 0 || level >= (int)p->pass_ms.size()) {
+    set_error("bad level");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  for (int k = 0; k < 4; ++k) {
+    if (out) out[k] = p->pass_ms[level][k];
+    if (launches) launches[k] = p->pass_launches[level][k];
+  }
   return PUCK_OK;
 }
 

@@ -148,6 +148,7 @@ class CompiledLevel:
     jobs: Dict[str, dict]            # per job: rules (rotated), segments, CSR tables
     unary_jobs: Dict[str, dict]
     viterbi: dict                    # backtrace tables
+    members: dict                    # coarse -> fine member lists (NT and T spaces)
 
     @property
     def n_nt(self) -> int:
@@ -310,6 +311,9 @@ def compile_level(g: Grammar, semiring: str = "viterbi") -> CompiledLevel:
     coarse_nt = nt_coarse
     coarse_t = t_coarse
 
+    nt_mem_off, nt_mem, nt_local = _coarse_members(coarse_nt, n_coarse)
+    t_mem_off, t_mem, t_local = _coarse_members(coarse_t, n_coarse)
+    members = dict(nt_mem_off=nt_mem_off, nt_mem=nt_mem, t_mem_off=t_mem_off, t_mem=t_mem)
     jobs: Dict[str, dict] = {}
     for name, bucket, rot, tgt_is_t, a_is_t, b_is_t in JOBS:
         rules = bucket_rules[bucket]
@@ -340,6 +344,9 @@ def compile_level(g: Grammar, semiring: str = "viterbi") -> CompiledLevel:
         rowptr = _csr(tgt, n_tgt, order)
         seg_bits = np.stack([s.bits for s in segments]).astype(np.int32) if segments \
             else np.zeros((0, mask_size), np.int32)
+        a_loc = t_local if a_is_t else nt_local
+        b_loc = t_local if b_is_t else nt_local
+        blocks = _pair_tables(tgt, ia, ib, scores, ac, bc, rule_seg, a_loc, b_loc, seg_bits, mask_size)
         jobs[name] = dict(
             bucket=bucket, rot=rot, tgt_is_t=tgt_is_t, a_is_t=a_is_t, b_is_t=b_is_t,
             tgt=tgt.astype(np.int32), ia=ia.astype(np.int32), ib=ib.astype(np.int32),
@@ -348,6 +355,7 @@ def compile_level(g: Grammar, semiring: str = "viterbi") -> CompiledLevel:
             rowptr=rowptr, csr_a=ia[order].astype(np.int32), csr_b=ib[order].astype(np.int32),
             csr_w=scores[order].astype(np.float32),
             csr_ac=ac[order].astype(np.int32), csr_bc=bc[order].astype(np.int32),
+            **blocks,
         )
 
     unary_jobs: Dict[str, dict] = {}
@@ -377,7 +385,60 @@ def compile_level(g: Grammar, semiring: str = "viterbi") -> CompiledLevel:
         bucket_rules=bucket_rules, bucket_scores=bucket_scores, bucket_ids=bucket_ids,
         nu_rules=nu_rules, nu_scores=nu_scores, tu_rules=tu_rules, tu_scores=tu_scores,
         lex_offsets=lex_offsets, lex_term=lex_term, lex_score=lex_score,
-        jobs=jobs, unary_jobs=unary_jobs, viterbi=viterbi)
+        jobs=jobs, unary_jobs=unary_jobs, viterbi=viterbi, members=members)
+
+
+PAIR_MIN_MEAN = 16      # the pair-factored layout pays off when coarse blocks hold this many rules
+
+
+def _coarse_members(coarse_of: np.ndarray, n_coarse: int):
+    """CSR from coarse symbol to its fine symbols (ascending) in one index space."""
+    order = np.argsort(coarse_of, kind="stable")
+    off = np.zeros(n_coarse + 1, np.int32)
+    np.cumsum(np.bincount(coarse_of, minlength=n_coarse), out=off[1:])
+    local = np.empty(coarse_of.shape[0], np.int32)
+    local[order] = np.arange(coarse_of.shape[0]) - off[coarse_of[order]]
+    return off, order.astype(np.int32), local
+
+
+def _pair_tables(tgt, ia, ib, w, ac, bc, rule_seg, a_local, b_local, seg_bits, mask_size) -> dict:
+    """Pair-factored layout for the device gather.
+
+    Rules are grouped by the coarse projection (ca, cb) of their two operands
+    ("pairs"), then by segment ("blocks"), then by target.  For one chart cell
+    the device computes, per live pair, the max-plus outer product
+    M[j][k] = max_s A_s[Y_j] + B_s[Z_k] over the pair's live splits once and
+    applies every rule of the pair as M[j][k] + w; a pair is skipped when no
+    staged split has a live Y on the left and a live Z on the right, which is
+    exact (every skipped term is the semiring zero).  ``pair_gate`` ORs the
+    segment bits of a pair's blocks so that pruned pairs are dropped before
+    any block is visited.  Rules are packed as ``j | k << 8 | target << 16``
+    with j, k the operands' positions among their coarse symbol's members.
+    """
+    n = tgt.shape[0]
+    if n == 0:
+        z = np.zeros(0, np.int32)
+        return dict(pair_mode=0, pair_key=z, pair_gate=z, pair_blk=np.zeros(1, np.int32), blk_seg=z,
+                    blk_ptr=np.zeros(1, np.int32), pair_rule=z, pair_w=np.zeros(0, np.float32))
+    pkey = (bc.astype(np.int64) << 8) | ac.astype(np.int64)
+    order = np.lexsort((b_local[ib], a_local[ia], tgt, rule_seg, pkey))
+    pk, sg = pkey[order], rule_seg[order]
+    pstart = np.flatnonzero(np.r_[True, pk[1:] != pk[:-1]])
+    bstart = np.flatnonzero(np.r_[True, (pk[1:] != pk[:-1]) | (sg[1:] != sg[:-1])])
+    npair, nblk = pstart.shape[0], bstart.shape[0]
+    pair_blk = np.searchsorted(bstart, np.r_[pstart, n]).astype(np.int32)
+    blk_seg = sg[bstart].astype(np.int32)
+    gate = np.zeros((npair, mask_size), np.int64)
+    pair_of_blk = np.repeat(np.arange(npair), np.diff(pair_blk))
+    np.bitwise_or.at(gate, pair_of_blk, seg_bits[blk_seg].astype(np.uint32).astype(np.int64))
+    packed = (a_local[ia[order]].astype(np.int64) | (b_local[ib[order]].astype(np.int64) << 8)
+              | (tgt[order].astype(np.int64) << 16))
+    mode = 2 if n / nblk >= PAIR_MIN_MEAN else 0
+    return dict(pair_mode=mode, pair_key=pk[pstart].astype(np.int32),
+                pair_gate=gate.astype(np.uint32).view(np.int32).reshape(-1).astype(np.int32),
+                pair_blk=pair_blk, blk_seg=blk_seg, blk_ptr=np.r_[bstart, n].astype(np.int32),
+                pair_rule=packed.astype(np.uint32).view(np.int32).astype(np.int32),
+                pair_w=w[order].astype(np.float32))
 
 
 def _viterbi_tables(n_nt, bucket_rules, bucket_scores, nu_rules, nu_scores, tu_rules, tu_scores) -> dict:

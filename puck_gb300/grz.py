@@ -54,6 +54,7 @@ def level_arrays(cl: CompiledLevel) -> Dict[str, np.ndarray]:
         "lex_off": cl.lex_offsets.astype(np.int64), "lex_term": cl.lex_term, "lex_score": cl.lex_score,
         "v_off": cl.viterbi["offsets"], "v_left": cl.viterbi["left"],
         "v_right": cl.viterbi["right"], "v_score": cl.viterbi["score"],
+        **cl.members,
     }
     for name, *_ in JOBS:
         j = cl.jobs[name]
@@ -65,6 +66,9 @@ def level_arrays(cl: CompiledLevel) -> Dict[str, np.ndarray]:
         out[f"{name}/bc"] = j["csr_bc"]
         out[f"{name}/tgt_seg"] = j["tgt_seg"]
         out[f"{name}/seg_bits"] = j["seg_bits"].reshape(-1)
+        out[f"{name}/pair_mode"] = np.asarray([j["pair_mode"]], np.int32)
+        for k in ("pair_key", "pair_gate", "pair_blk", "blk_seg", "blk_ptr", "pair_rule", "pair_w"):
+            out[f"{name}/{k}"] = j[k]
         # rule-order form and sub-segments (the oracle's view)
         out[f"{name}/tgt"] = j["tgt"]
         out[f"{name}/ia"] = j["ia"]

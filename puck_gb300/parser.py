@@ -306,6 +306,14 @@ class CLParser:
         _lib.check(self._L.puck_parser_stats(self._p, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in s._fields_}
 
+    def pass_ms(self, level: int):
+        """Per-level [inside, outside, masks, decode] CUDA-event ms and launch
+        counts of the last call."""
+        ms = (ctypes.c_double * 4)()
+        n = (ctypes.c_int64 * 4)()
+        _lib.check(self._L.puck_parser_pass_ms(self._p, level, ms, n))
+        return list(ms), list(n)
+
     def release(self) -> None:
         if getattr(self, "_p", None):
             self._L.puck_parser_destroy(self._p)
