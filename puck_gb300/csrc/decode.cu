@@ -10,7 +10,7 @@
 //   root scores   src/main/scala/puck/parser/gen/CLParserUtils.scala:305-316,
 //                 CLParser.scala:189-206
 
-#include "device_common.cuh"
+#include "mbr_dp.cuh"
 
 namespace puck {
 namespace {
@@ -195,63 +195,8 @@ __global__ void k_mbr_decode(DevBatch B, DevMask M, int scaling, const float2* d
                              float* scratch, DevNode* nodes) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= B.nsent) return;
-  const int n = B.len[s];
-  const long long off = B.cell_off[s], toff = off + tri(n);
-  // per-sentence scratch: best scores, best splits, unary flags ((n+1)^2 each)
-  float* bs = scratch + mbr_off[s];
-  int* bsplit = reinterpret_cast<int*>(bs + (n + 1) * (n + 1));
-  int* uu = bsplit + (n + 1) * (n + 1);
-  auto idx = [n](int x, int y) { return x * (n + 1) + y; };
-  const float root_i = scaling ? M.iscale[toff + chart_index(0, n, n)] : 0.f;
-  for (int span = 1; span <= n; ++span) {
-    for (int bg = 0; bg + span <= n; ++bg) {
-      const int en = bg + span;
-      const long long ct = toff + chart_index(bg, en, n), cb = off + chart_index(bg, en, n);
-      float topS = decode[ct].x, botS = decode[cb].x;
-      if (scaling) {
-        topS *= (float)exp((double)M.iscale[ct] + (double)M.oscale[ct] - (double)root_i);
-        botS *= (float)exp((double)M.iscale[cb] + (double)M.oscale[cb] - (double)root_i);
-      }
-      if (isnan(topS)) topS = 0.f;
-      if (isnan(botS)) botS = 0.f;
-      topS = fminf(topS, 1.0f);
-      botS = fminf(botS, 1.0f);
-      const bool useU = (bg + 1 < en) || (double)topS > 0.4;
-      uu[idx(bg, en)] = useU;
-      float sc = useU ? topS + botS : botS;
-      if (span > 1) {
-        float bss = 0.0f;
-        int bsp = bg + 1;
-        for (int sp = bg + 1; sp < en; ++sp) {
-          const float v = bs[idx(bg, sp)] + bs[idx(sp, en)];
-          if (v > bss) { bsp = sp; bss = v; }
-        }
-        bsplit[idx(bg, en)] = bsp;
-        sc += bss;
-      }
-      bs[idx(bg, en)] = sc;
-    }
-  }
-  DevNode* out = nodes + B.node_off[s];
-  int stack_b[kMaxLen], stack_e[kMaxLen];
-  int top = 0, p = 0;
-  stack_b[0] = 0; stack_e[0] = n; top = 1;
-  while (top > 0) {
-    --top;
-    const int bg = stack_b[top], en = stack_e[top];
-    const long long ct = toff + chart_index(bg, en, n), cb = off + chart_index(bg, en, n);
-    DevNode nd;
-    nd.top = uu[idx(bg, en)] ? __float_as_int(decode[ct].y) : -1;
-    nd.bot = __float_as_int(decode[cb].y);
-    nd.width = en - bg;
-    nd.score = bs[idx(bg, en)];
-    out[p++] = nd;
-    if (en - bg > 1) {
-      const int sp = bsplit[idx(bg, en)];
-      stack_b[top] = sp; stack_e[top] = en; ++top;
-      stack_b[top] = bg; stack_e[top] = sp; ++top;
-    }
-  }
+  mbr_decode_sentence(B.len[s], B.cell_off[s], decode, M.iscale, M.oscale, scaling, scratch + mbr_off[s],
+                      nodes + B.node_off[s]);
 }
 
 // log Z per sentence (CLParser.scala:189-206), accumulated in FP64.
