@@ -133,6 +133,26 @@ puck_status puck_parser_stats(const puck_parser* p, puck_stats* out);
  * launches[0..3] the matching kernel launch counts. */
 puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[4], int64_t launches[4]);
 
+/* Max-constituent (MBR) tree decode into caller-owned device buffers with no
+ * device allocation, for callers that cannot allocate at the point where they
+ * decode: a host running inside a device arena its own pool carved out, a
+ * serving loop that must keep the CUDA allocator off its request path, or
+ * work issued while another framework captures the stream.  No counterpart in
+ * the reference (its MBR decode runs on the host, CLParser.scala:589-696).
+ * Same decode as puck_parse's MBR path: cell_decode (device) holds per cell
+ * {best coarse marginal, coarse symbol as int bits} -- the layout
+ * puck_debug_copy(which = 5) returns; iscale/oscale (device, per cell) are the
+ * coarse level's log-scales for a Real fine level, or both NULL; lengths is a
+ * host array; nodes (device) receives sum(2*len_i - 1) preorder nodes.  Work
+ * is enqueued on `stream` (a cudaStream_t, NULL = default stream).  Scratch
+ * lives in a fixed array in the library's device memory: at most 65,536
+ * sentences and sum of 3*(len_i+1)^2 <= 4,194,304 floats per call (larger
+ * calls are rejected with PUCK_ERR_INVALID_ARG); the first call on a device
+ * resolves the array's address and should precede any stream capture; calls
+ * whose work overlaps on the GPU race on the array. */
+puck_status puck_mbr_decode_static(const float* cell_decode, const float* iscale, const float* oscale,
+                                   const int32_t* lengths, int32_t nsent, puck_tree_node* nodes, void* stream);
+
 /* Last error message of the calling thread; returns the full length. */
 size_t puck_last_error(char* buf, size_t len);
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <string>
 
 namespace puck {
 
@@ -133,6 +134,10 @@ cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevMa
                                const double* part_scale, float* log_z, cudaStream_t st);
 
 size_t pass_smem_bytes(const DevLevel& L, int chunk);
+
+// Message returned by puck_last_error on the calling thread.
+void set_last_error(const char* msg);
+inline void set_last_error(const std::string& msg) { set_last_error(msg.c_str()); }
 int pick_split_chunk(int cell_size, int max_len);
 
 }  // namespace puck

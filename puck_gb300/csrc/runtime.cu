@@ -131,6 +131,8 @@ std::vector<std::string> split_lines(const std::string& s) {
 
 }  // namespace
 
+void puck::set_last_error(const char* msg) { set_error(msg); }
+
 struct puck_grammar {
   std::vector<HostLevel> levels;
   std::unordered_map<std::string, int> word_index;
