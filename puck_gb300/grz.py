@@ -94,10 +94,16 @@ def level_arrays(cl: CompiledLevel) -> Dict[str, np.ndarray]:
     return {k: np.ascontiguousarray(v) for k, v in out.items()}
 
 
+def _entry(z: zipfile.ZipFile, name: str, data: bytes) -> None:
+    info = zipfile.ZipInfo(name, date_time=(1980, 1, 1, 0, 0, 0))   # fixed: same grammar, same bytes
+    info.compress_type = zipfile.ZIP_STORED
+    z.writestr(info, data)
+
+
 def write_sequence(path: str, levels: Sequence[CompiledLevel]) -> None:
     names = [f"parser-{i}" for i in range(len(levels))]
     with zipfile.ZipFile(path, "w", compression=zipfile.ZIP_STORED) as z:
-        z.writestr("parserNames", "\n".join(names).encode("utf-8"))
+        _entry(z, "parserNames", "\n".join(names).encode("utf-8"))
         for name, cl in zip(names, levels):
             g = cl.grammar
             hdr = {
@@ -105,13 +111,13 @@ def write_sequence(path: str, levels: Sequence[CompiledLevel]) -> None:
                 "cell_size": cl.cell_size, "mask_size": cl.mask_size, "n_coarse": cl.n_coarse,
                 "root": cl.root, "n_words": len(g.words), "name": g.name,
             }
-            z.writestr(f"{name}/header", "".join(f"{k} {v}\n" for k, v in hdr.items()).encode("utf-8"))
+            _entry(z, f"{name}/header", "".join(f"{k} {v}\n" for k, v in hdr.items()).encode("utf-8"))
             for k, a in level_arrays(cl).items():
-                z.writestr(f"{name}/arrays/{k}", _arr_bytes(a))
-            z.writestr(f"{name}/nt_names.txt", "\n".join(g.labels[i] for i in cl.nt_labels).encode("utf-8"))
-            z.writestr(f"{name}/t_names.txt", "\n".join(g.labels[i] for i in cl.t_labels).encode("utf-8"))
-            z.writestr(f"{name}/coarse_names.txt", "\n".join(g.coarse_names).encode("utf-8"))
-            z.writestr(f"{name}/words.txt", "\n".join(g.words).encode("utf-8"))
+                _entry(z, f"{name}/arrays/{k}", _arr_bytes(a))
+            _entry(z, f"{name}/nt_names.txt", "\n".join(g.labels[i] for i in cl.nt_labels).encode("utf-8"))
+            _entry(z, f"{name}/t_names.txt", "\n".join(g.labels[i] for i in cl.t_labels).encode("utf-8"))
+            _entry(z, f"{name}/coarse_names.txt", "\n".join(g.coarse_names).encode("utf-8"))
+            _entry(z, f"{name}/words.txt", "\n".join(g.words).encode("utf-8"))
 
 
 class LevelInfo:
