@@ -17,6 +17,12 @@ Reported (one JSON line on rank 0):
   roofline  the fine-level inside span kernel (the dominant kernel)
   cpu_baseline  the CPU oracle (a port of the reference algorithm) on a
           bounded sample, all host threads
+  plain   the same library run one sentence at a time (max_batch_sentences=1)
+          on a bounded sample: the plain CUDA CKY path the batched and served
+          paths are compared with
+  serving the continuous-batching server under open-loop Poisson arrivals
+          (lengths lognormal mean 23 clipped 1-60): achieved sentences/s and
+          p50/p99 latency per offered rate
 
 ``--impl reference`` times the reference's algorithm on the host cores (the
 oracle port: the reference's own JVM/OpenCL stack cannot run on this machine).
@@ -129,6 +135,107 @@ def cpu_baseline(levels, sents, sample: int):
                       f"fine inside, backtrace; {dt:.1f}s"}
 
 
+def plain_baseline(path, sents, sample: int, device: int):
+    """The library one sentence at a time: every span launch covers the
+    cells of a single sentence."""
+    from puck_gb300.parser import CLParser, pack_sentences
+    P = CLParser(path, max_alloc_size=8 << 30, profile=True, device=device, max_length=MAX_LEN,
+                 max_batch_sentences=1)
+    sub = sents[:sample]
+    words, offsets, _ = pack_sentences(sub)
+    P.parse_ids(*pack_sentences(sub[:4])[:2])  # warm-up
+    t0 = time.perf_counter()
+    nodes, st = P.parse_ids(words, offsets)
+    dt = time.perf_counter() - t0
+    assert (st == 0).all()
+    s = P.stats()
+    P.release()
+    return {"value": round(len(sub) / (s["ms_device"] / 1e3), 2), "unit": "sentences/s",
+            "e2e": round(len(sub) / dt, 2),
+            "sample": f"first {len(sub)} sentences of the workload, one batch per sentence (device time)"}
+
+
+def serving(path, levels, args, device: int):
+    """Open-loop Poisson arrivals into the continuous-batching server."""
+    import threading
+    import numpy as np
+    from puck_gb300 import synth
+    from puck_gb300.parser import pack_sentences
+    from puck_gb300.server import CLServer, now_ns
+    n = args.serve_sentences
+    sents = synth.lognormal_sentences(args.seed + 1000, n, 23, 1, 60, len(levels[1].words))
+    words, offsets, lens = pack_sentences(sents)
+    S = CLServer(path, max_alloc_size=args.serve_mem_gb << 30, device=device, max_length=60, collect=False)
+
+    def drain(count, want):
+        lat, done_at = [], []
+        while len(lat) < count:
+            for rid in S.poll(8192, 20):
+                nodes, st, ln = S.take(int(rid), want[int(rid)])
+                assert st == 0
+                lat.append(ln)
+        return np.array(lat, np.int64)
+
+    # warm-up: a few hundred sentences at once
+    w0, o0, l0 = pack_sentences(sents[:256])
+    ids = S.submit_ids(w0, o0)
+    drain(len(ids), {int(i): int(k) for i, k in zip(ids, l0)})
+    rows = []
+    rng = np.random.default_rng(args.seed + 2000)
+    for rate in args.serve_rates:
+        gaps = rng.exponential(1.0 / rate, n)
+        st0 = S.stats()
+        t0 = now_ns() + 2_000_000
+        sched = t0 + np.cumsum(gaps * 1e9).astype(np.int64)
+        want = {}
+        lock = threading.Lock()
+
+        def gen():
+            i = 0
+            while i < n:
+                t = now_ns()
+                j = int(np.searchsorted(sched, t, side="right"))
+                if j > i:
+                    o = offsets[i:j + 1] - offsets[i]
+                    w = words[offsets[i]:offsets[j]]
+                    with lock:
+                        rid = S.submit_ids(w, o, sched[i:j])
+                        for k, r in enumerate(rid):
+                            want[int(r)] = int(lens[i + k])
+                    i = j
+                else:
+                    time.sleep(min(2e-4, max((sched[i] - t) / 1e9, 0)))
+
+        th = threading.Thread(target=gen)
+        th.start()
+        lat, got = [], 0
+        t_last = t0
+        while got < n:
+            for rid in S.poll(8192, 20):
+                with lock:
+                    ln_ = want[int(rid)]
+                nodes, st, ln = S.take(int(rid), ln_)
+                assert st == 0
+                lat.append(ln)
+                got += 1
+            t_last = now_ns()
+        th.join()
+        st1 = S.stats()
+        lat = np.array(lat, np.float64) / 1e6
+        span_s = (t_last - t0) / 1e9
+        rows.append({"offered": rate, "achieved": round(n / span_s, 1),
+                     "p50_ms": round(float(np.percentile(lat, 50)), 2),
+                     "p99_ms": round(float(np.percentile(lat, 99)), 2),
+                     "resident_peak": int(st1["resident_peak"]),
+                     "ticks": int(st1["ticks"] - st0["ticks"]),
+                     "gpu_ms": round(st1["ms_device"] - st0["ms_device"], 1)})
+        log(f"serving {rate}/s: {rows[-1]}")
+    S.close()
+    return {"sentences_per_rate": n, "lengths": "lognormal mean 23 clipped 1-60",
+            "arrivals": "open-loop Poisson, latency from scheduled arrival to result available on the host",
+            "rates": rows}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -197,7 +304,9 @@ def run_ours(args):
     pk = peaks()
     sm_max = float(pk.get("sm_max_mhz", 2070.0))
     fp32_peak = 152 * 128 * sm_max * 1e6 / 1e12                 # FP32 lane-ops/s in T
-    per_launch_ops = 3.0 * work / max(fine_in_launch, 1)         # (L+R)+w and max per (rule, split)
+    # split-factored work units: each (live split, child pair) element of M and
+    # each applied rule is one add and one max
+    per_launch_ops = 2.0 * work / max(fine_in_launch, 1)
     avg_launch_s = fine_in_ms / 1e3 / max(fine_in_launch, 1)
     achieved = per_launch_ops / avg_launch_s / 1e12
     out = {
@@ -220,18 +329,24 @@ def run_ours(args):
         "roofline": {"bound": "alu", "kernel": "k_inside_span<viterbi> (fine level)",
                      "achieved": round(achieved, 3), "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
                      "frac": round(achieved / fp32_peak, 4), "traffic": None,
-                     "note": "FP32 max-plus on CUDA cores: 3 ops per executed (rule, split); peak = 152 SMs x "
-                             "128 FP32 lanes x measured max SM clock",
+                     "note": "FP32 max-plus on CUDA cores: ops = 2 x (sum over cells of live splits x child "
+                             "pairs + applied rules); peak = 152 SMs x 128 FP32 lanes x measured max SM clock",
                      "work_per_launch": round(work / max(fine_in_launch, 1)),
                      "avg_launch_ms": round(avg_launch_s * 1e3, 4)},
         "passes_ms_last_step": {
             f"level{l}": [round(v, 2) for v in P.pass_ms(l)[0]] for l in range(len(levels))},
     }
-    if rank == 0 and world == 1 and args.cpu_sample > 0:
-        out["cpu_baseline"] = cpu_baseline(levels, sents, args.cpu_sample)
+    P.release()
+    if rank == 0 and world == 1:
+        if args.cpu_sample > 0:
+            out["cpu_baseline"] = cpu_baseline(levels, sents, args.cpu_sample)
+        if args.plain_sample > 0:
+            out["plain"] = plain_baseline(path, sents, args.plain_sample, local)
+            out["plain"]["batched_over_plain"] = round(value / out["plain"]["value"], 2)
+        if args.serve_rates:
+            out["serving"] = serving(path, levels, args, local)
     if rank == 0:
         print(json.dumps(out), flush=True)
-    P.release()
     os.unlink(path)
 
 
@@ -282,6 +397,10 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=32)
     ap.add_argument("--seed", type=int, default=2)
     ap.add_argument("--mem-gb", type=int, default=160)
+    ap.add_argument("--plain-sample", type=int, default=100)
+    ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x], default="1000,2000,3000")
+    ap.add_argument("--serve-sentences", type=int, default=6000)
+    ap.add_argument("--serve-mem-gb", type=int, default=32)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

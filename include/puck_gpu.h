@@ -153,6 +153,53 @@ puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[
 puck_status puck_mbr_decode_static(const float* cell_decode, const float* iscale, const float* oscale,
                                    const int32_t* lengths, int32_t nsent, puck_tree_node* nodes, void* stream);
 
+/* --- continuous-batching server ------------------------------------------
+ * Replaces the reference's batching front for parse requests,
+ * BatchFunctionAnnotatorService (src/main/scala/puck/AnnotatorService.scala:
+ * 29-78, one future per sentence, batches flushed by time or size), with
+ * continuous batching: a request loop admits sentences as chart memory and
+ * slots free up, keeps every admitted sentence's charts and pruning masks
+ * resident on the device, and advances all resident sentences together, one
+ * pass step per sentence per tick, each kernel of a tick covering the cells
+ * of every sentence at that step (sentences at different span lengths share
+ * one launch).  Options as for puck_parser_create: mem_bytes sizes the chart
+ * arena, max_batch_sentences caps the resident sentences (0: 65,536),
+ * max_length, decode and prune_threshold as for a parse.  submit, poll, take
+ * and stats may be called from any thread.  A result does not depend on which
+ * other sentences were resident; a one-word sentence parses as in a batch
+ * that also holds longer sentences. */
+typedef struct puck_server puck_server;
+
+typedef struct puck_server_stats {
+  int64_t submitted, completed, failed;
+  int64_t ticks, kernel_launches;
+  int64_t resident, resident_peak;       /* sentences holding charts now / at most */
+  int64_t arena_cells, arena_cells_peak; /* chart arena capacity / most cells in use */
+  double ms_device;                      /* CUDA-event time of all ticks */
+  int64_t h2d_bytes, d2h_bytes;
+} puck_server_stats;
+
+puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts, puck_status* status);
+/* Finishes every admitted request, then stops the request loop. */
+void puck_server_destroy(puck_server* s);
+/* Clock of arrival and latency times (monotonic, nanoseconds). */
+int64_t puck_server_now_ns(void);
+/* Queues sentences i = 0..nsent-1 (word_ids[offsets[i] .. offsets[i+1])).
+ * arrival_ns[i] is the time each request's latency counts from (NULL or 0:
+ * now).  ids[i] receives the request id.  A sentence that cannot be parsed
+ * (empty, too long, unknown word) still gets an id; its result carries the
+ * failure status. */
+puck_status puck_server_submit(puck_server* s, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                               const int64_t* arrival_ns, int64_t* ids);
+/* Waits up to wait_ms for finished requests and writes up to max_ids of their
+ * ids (each id once); returns how many. */
+int32_t puck_server_poll(puck_server* s, int64_t* ids, int32_t max_ids, int32_t wait_ms);
+/* Copies a finished request's 2n-1 tree nodes (as puck_parse) and releases
+ * it; sent_status and latency_ns (completion minus arrival) may be NULL. */
+puck_status puck_server_take(puck_server* s, int64_t id, puck_tree_node* nodes, int32_t max_nodes,
+                             int32_t* sent_status, int64_t* latency_ns);
+puck_status puck_server_get_stats(const puck_server* s, puck_server_stats* out);
+
 /* Last error message of the calling thread; returns the full length. */
 size_t puck_last_error(char* buf, size_t len);
 

@@ -42,10 +42,20 @@ class Stats(ctypes.Structure):
                 ("ms_device", ctypes.c_double), ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
 
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("ticks", ctypes.c_int64), ("kernel_launches", ctypes.c_int64), ("resident", ctypes.c_int64),
+                ("resident_peak", ctypes.c_int64), ("arena_cells", ctypes.c_int64),
+                ("arena_cells_peak", ctypes.c_int64), ("ms_device", ctypes.c_double),
+                ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
+
+
 EXPORTS = ("puck_default_options", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
            "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
-           "puck_parser_stats", "puck_parser_pass_ms", "puck_last_error")
+           "puck_parser_stats", "puck_parser_pass_ms", "puck_mbr_decode_static", "puck_server_create",
+           "puck_server_destroy", "puck_server_now_ns", "puck_server_submit", "puck_server_poll",
+           "puck_server_take", "puck_server_get_stats", "puck_last_error")
 
 _lib = None
 _lock = threading.Lock()
@@ -88,6 +98,19 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_parser_stats.restype = I
         L.puck_parser_pass_ms.argtypes = [P, I, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(I64)]
         L.puck_parser_pass_ms.restype = I
+        L.puck_server_create.restype = P
+        L.puck_server_create.argtypes = [P, ctypes.POINTER(Options), ctypes.POINTER(I)]
+        L.puck_server_destroy.argtypes = [P]
+        L.puck_server_now_ns.argtypes = []
+        L.puck_server_now_ns.restype = I64
+        L.puck_server_submit.argtypes = [P, P, P, I, P, P]
+        L.puck_server_submit.restype = I
+        L.puck_server_poll.argtypes = [P, P, I, I]
+        L.puck_server_poll.restype = I
+        L.puck_server_take.argtypes = [P, I64, P, I, ctypes.POINTER(I), ctypes.POINTER(I64)]
+        L.puck_server_take.restype = I
+        L.puck_server_get_stats.argtypes = [P, ctypes.POINTER(ServerStats)]
+        L.puck_server_get_stats.restype = I
         L.puck_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         L.puck_last_error.restype = ctypes.c_size_t
         _lib = L

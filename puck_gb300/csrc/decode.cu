@@ -19,13 +19,27 @@ using namespace dev;
 
 // ---------------------------------------------------------------------------
 // Pruning masks: one warp per cell (max-marginal test against root + thresh).
-__global__ void k_masks(DevLevel L, DevBatch B, const float* inside, const float* outside, float thresh,
+// Cell c of sentence s (unit i of a per-cell work list).
+struct CellRef { int s; long long c, first, last; };
+__device__ __forceinline__ CellRef cell_ref(const DevBatch& B, const DevWork& W, int i) {
+  const int k = entry_of(W, i);
+  CellRef r;
+  r.s = W.sent[k];
+  const int n = B.len[r.s];
+  r.first = B.cell_off[r.s];
+  r.last = r.first + 2 * tri(n);
+  r.c = r.first + (i - W.pref[k]);
+  return r;
+}
+
+__global__ void k_masks(DevLevel L, DevBatch B, DevWork W, const float* inside, const float* outside, float thresh,
                         int* out) {
-  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long unit = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (c >= B.num_cells) return;
-  const int s = sentence_of_cell(B, c);
-  const long long first = B.cell_off[s], last = B.cell_off[s + 1];
+  if (unit >= W.nunits) return;
+  const CellRef R = cell_ref(B, W, (int)unit);
+  const int s = R.s;
+  const long long c = R.c, first = R.first, last = R.last;
   const int cs = L.cell_size;
   const float root_score = inside[(last - 1) * cs + L.root];
   const float cutoff = root_score + thresh;
@@ -50,10 +64,11 @@ __global__ void k_masks(DevLevel L, DevBatch B, const float* inside, const float
 }
 
 // Per-cell log-scale: max over the cell, -9000 floor mapped to 0.
-__global__ void k_scaling(int cs, long long num_cells, const float* chart, float* out) {
-  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_scaling(int cs, DevBatch B, DevWork W, const float* chart, float* out) {
+  const long long unit = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (c >= num_cells) return;
+  if (unit >= W.nunits) return;
+  const long long c = cell_ref(B, W, (int)unit).c;
   float m = -100000.0f;
   for (int k = lane; k < cs; k += 32) m = fmaxf(chart[c * cs + k], m);
   m = warp_reduce<SEMI_VITERBI>(m);
@@ -80,14 +95,15 @@ __device__ __forceinline__ Best warp_argmax_last(Best v) {
   return v;
 }
 
-__global__ void k_viterbi(DevLevel L, DevBatch B, const float* inside, DevNode* nodes) {
+__global__ void k_viterbi(DevLevel L, DevBatch B, DevWork W, int max_len, const float* inside, DevNode* nodes) {
   extern __shared__ DevNode tn_all[];
   const int lane = threadIdx.x & 31;
   const int wib = threadIdx.x >> 5;
-  const int s = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  if (s >= B.nsent) return;
+  const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (k >= W.nent) return;
+  const int s = W.sent[k];
   const int n = B.len[s];
-  DevNode* tn = tn_all + wib * (2 * B.max_len - 1);
+  DevNode* tn = tn_all + wib * (2 * max_len - 1);
   const int cs = L.cell_size;
   const float* ibot = inside + B.cell_off[s] * cs;
   const float* itop = ibot + tri(n) * cs;
@@ -158,16 +174,18 @@ __global__ void k_viterbi(DevLevel L, DevBatch B, const float* inside, DevNode* 
 // MBR: per cell best coarse marginal (warp per cell), then a per-sentence
 // max-constituent CKY with on-device extraction.
 template <int S>
-__global__ void k_mbr_cells(DevLevel L, DevBatch B, const float* inside, const float* outside, float2* decode) {
+__global__ void k_mbr_cells(DevLevel L, DevBatch B, DevWork W, const float* inside, const float* outside,
+                            float2* decode) {
   extern __shared__ float margs_all[];
-  const long long c = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long unit = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   float* margs = margs_all + wib * L.n_coarse;
-  if (c >= B.num_cells) return;
+  if (unit >= W.nunits) return;
   for (int k = lane; k < L.n_coarse; k += 32) margs[k] = 0.f;
   __syncwarp();
-  const int s = sentence_of_cell(B, c);
-  const long long first = B.cell_off[s], last = B.cell_off[s + 1];
+  const CellRef R = cell_ref(B, W, (int)unit);
+  const int s = R.s;
+  const long long c = R.c, first = R.first, last = R.last;
   const int cs = L.cell_size;
   const float root_score = inside[(last - 1) * cs + L.root];
   const bool term = (c - first) < B.len[s];
@@ -191,19 +209,21 @@ __global__ void k_mbr_cells(DevLevel L, DevBatch B, const float* inside, const f
   if (lane == 0) decode[c] = make_float2(best, __int_as_float(bsym));
 }
 
-__global__ void k_mbr_decode(DevBatch B, DevMask M, int scaling, const float2* decode, const long long* mbr_off,
-                             float* scratch, DevNode* nodes) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= B.nsent) return;
+__global__ void k_mbr_decode(DevBatch B, DevWork W, DevMask M, int scaling, const float2* decode,
+                             const long long* mbr_off, float* scratch, DevNode* nodes) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= W.nent) return;
+  const int s = W.sent[k];
   mbr_decode_sentence(B.len[s], B.cell_off[s], decode, M.iscale, M.oscale, scaling, scratch + mbr_off[s],
                       nodes + B.node_off[s]);
 }
 
 // log Z per sentence (CLParser.scala:189-206), accumulated in FP64.
-__global__ void k_root_scores(DevLevel L, DevBatch B, DevMask M, const float* inside, const double* part_scale,
-                              float* log_z) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= B.nsent) return;
+__global__ void k_root_scores(DevLevel L, DevBatch B, DevWork W, DevMask M, const float* inside,
+                              const double* part_scale, float* log_z) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= W.nent) return;
+  const int s = W.sent[k];
   const int n = B.len[s];
   const long long root_cell = B.cell_off[s] + tri(n) + chart_index(0, n, n);
   const float v = inside[root_cell * L.cell_size + L.root];
@@ -222,59 +242,60 @@ void set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
-cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
-                         float thresh, int* masks_out, cudaStream_t st) {
-  const long long threads = B.num_cells * 32;
-  const int blocks = (int)((threads + 255) / 256);
+cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const DevWork& W, const float* inside,
+                         const float* outside, float thresh, int* masks_out, cudaStream_t st) {
+  const int blocks = (int)((W.nunits * 32 + 255) / 256);
   if (blocks == 0) return cudaSuccess;
-  k_masks<<<blocks, 256, 0, st>>>(L, B, inside, outside, thresh, masks_out);
+  k_masks<<<blocks, 256, 0, st>>>(L, B, W, inside, outside, thresh, masks_out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_scaling(int cell_size, long long num_cells, const float* chart, float* out, cudaStream_t st) {
-  const int blocks = (int)((num_cells * 32 + 255) / 256);
-  if (blocks == 0) return cudaSuccess;
-  k_scaling<<<blocks, 256, 0, st>>>(cell_size, num_cells, chart, out);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const float* inside, DevNode* nodes,
+cudaError_t launch_scaling(int cell_size, const DevBatch& B, const DevWork& W, const float* chart, float* out,
                            cudaStream_t st) {
-  const int wpb = 4;
-  const int blocks = (B.nsent + wpb - 1) / wpb;
+  const int blocks = (int)((W.nunits * 32 + 255) / 256);
   if (blocks == 0) return cudaSuccess;
-  const size_t smem = (size_t)wpb * (2 * B.max_len - 1) * sizeof(DevNode);
-  set_smem(k_viterbi, smem);
-  k_viterbi<<<blocks, wpb * 32, smem, st>>>(L, B, inside, nodes);
+  k_scaling<<<blocks, 256, 0, st>>>(cell_size, B, W, chart, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mbr_cells(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
-                             float2* decode, cudaStream_t st) {
+cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const DevWork& W, int max_len, const float* inside,
+                           DevNode* nodes, cudaStream_t st) {
+  const int wpb = 4;
+  const int blocks = (W.nent + wpb - 1) / wpb;
+  if (blocks == 0) return cudaSuccess;
+  const size_t smem = (size_t)wpb * (2 * max_len - 1) * sizeof(DevNode);
+  set_smem(k_viterbi, smem);
+  k_viterbi<<<blocks, wpb * 32, smem, st>>>(L, B, W, max_len, inside, nodes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mbr_cells(const DevLevel& L, const DevBatch& B, const DevWork& W, const float* inside,
+                             const float* outside, float2* decode, cudaStream_t st) {
   const int wpb = 8;
-  const int blocks = (int)((B.num_cells + wpb - 1) / wpb);
+  const int blocks = (int)((W.nunits + wpb - 1) / wpb);
   if (blocks == 0) return cudaSuccess;
   const size_t smem = (size_t)wpb * L.n_coarse * sizeof(float);
   if (L.semiring == SEMI_LOGSUM)
-    k_mbr_cells<SEMI_LOGSUM><<<blocks, wpb * 32, smem, st>>>(L, B, inside, outside, decode);
+    k_mbr_cells<SEMI_LOGSUM><<<blocks, wpb * 32, smem, st>>>(L, B, W, inside, outside, decode);
   else
-    k_mbr_cells<SEMI_REAL><<<blocks, wpb * 32, smem, st>>>(L, B, inside, outside, decode);
+    k_mbr_cells<SEMI_REAL><<<blocks, wpb * 32, smem, st>>>(L, B, W, inside, outside, decode);
   return cudaGetLastError();
 }
 
-cudaError_t launch_mbr_decode(const DevBatch& B, const DevMask& M, int scaling, const float2* decode,
-                              const long long* mbr_off, float* scratch, DevNode* nodes, cudaStream_t st) {
-  const int blocks = (B.nsent + 63) / 64;
+cudaError_t launch_mbr_decode(const DevBatch& B, const DevWork& W, const DevMask& M, int scaling,
+                              const float2* decode, const long long* mbr_off, float* scratch, DevNode* nodes,
+                              cudaStream_t st) {
+  const int blocks = (W.nent + 63) / 64;
   if (blocks == 0) return cudaSuccess;
-  k_mbr_decode<<<blocks, 64, 0, st>>>(B, M, scaling, decode, mbr_off, scratch, nodes);
+  k_mbr_decode<<<blocks, 64, 0, st>>>(B, W, M, scaling, decode, mbr_off, scratch, nodes);
   return cudaGetLastError();
 }
 
-cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevMask& M, const float* inside,
-                               const double* part_scale, float* log_z, cudaStream_t st) {
-  const int blocks = (B.nsent + 127) / 128;
+cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                               const float* inside, const double* part_scale, float* log_z, cudaStream_t st) {
+  const int blocks = (W.nent + 127) / 128;
   if (blocks == 0) return cudaSuccess;
-  k_root_scores<<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, log_z);
+  k_root_scores<<<blocks, 128, 0, st>>>(L, B, W, M, inside, part_scale, log_z);
   return cudaGetLastError();
 }
 

@@ -19,27 +19,17 @@ __device__ __forceinline__ int chart_index(int b, int e, int n) {
   return min(b, e) + sp * n - sp * (sp - 1) / 2;
 }
 
-struct SentCell { int s, b; };
-
-// i-th cell of span length `span` over the batch (sentences longest first).
-__device__ __forceinline__ SentCell span_cell(const DevBatch& B, int span, int i) {
-  const int* pref = B.span_pref + B.span_base[span];
-  int lo = 0, hi = B.span_count[span];
+// Entry k of a work list holding unit i (pref[k] <= i < pref[k+1]).
+__device__ __forceinline__ int entry_of(const DevWork& W, int i) {
+  int lo = 0, hi = W.nent;
   while (hi - lo > 1) {
     int mid = (lo + hi) >> 1;
-    if (pref[mid] <= i) lo = mid; else hi = mid;
-  }
-  return {B.order[lo], i - pref[lo]};
-}
-
-__device__ __forceinline__ int sentence_of_cell(const DevBatch& B, long long c) {
-  int lo = 0, hi = B.nsent;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (B.cell_off[mid] <= c) lo = mid; else hi = mid;
+    if (W.pref[mid] <= i) lo = mid; else hi = mid;
   }
   return lo;
 }
+
+__device__ __forceinline__ int span_of(const DevWork& W, int k) { return W.span ? W.span[k] : W.span_all; }
 
 // Semirings (src/main/scala/puck/parser/RuleSemiring.scala:22-98).
 template <int S> struct Sr;

@@ -385,18 +385,20 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 }
 
 // ---------------------------------------------------------------------------
-// Inside pass for one span length (span 1: the unary layer over lexicon cells).
+// Inside pass over the cells of a work list (span 1: the unary layer over
+// lexicon cells).  Register budgets: five CTAs per SM for the pair-factored
+// mode, six for the target-major mode (the Viterbi instances without spills).
 template <int S, int MODE>
-__global__ void __launch_bounds__(256) k_inside_span(DevLevel L, DevBatch B, DevMask M, int span, float* inside,
-                                                     DevLive V, Counters C, int chunk) {
+__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
+    k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
   const Smem sm = carve(smem, L, chunk);
   float* P = sm.P;
   float* Q = sm.Q;
-  const SentCell sc = span_cell(B, span, blockIdx.x);
-  const int s = sc.s, b = sc.b, e = b + span, n = B.len[s];
+  const int ent = entry_of(W, blockIdx.x);
+  const int s = W.sent[ent], span = span_of(W, ent), b = (int)blockIdx.x - W.pref[ent], e = b + span, n = B.len[s];
   const long long off = B.cell_off[s], toff = off + tri(n);
   const long long pbot = off + chart_index(b, e, n), ptop = toff + chart_index(b, e, n);
   if (threadIdx.x == 0) {
@@ -452,21 +454,21 @@ __global__ void __launch_bounds__(256) k_inside_span(DevLevel L, DevBatch B, Dev
 }
 
 // ---------------------------------------------------------------------------
-// Outside pass for one span length: outside-top of each cell gathered from its
+// Outside pass over the cells of a work list: outside-top of each cell gathered from its
 // parents, then the unary layer to outside-bot (and, at span 1, the
 // terminal-child binaries that the reference runs after its span loop).
 template <int S, int MODE>
-__global__ void __launch_bounds__(256) k_outside_span(DevLevel L, DevBatch B, DevMask M, int span,
-                                                      const float* inside, float* outside, DevLive V, Counters C,
-                                                      int chunk) {
+__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
+    k_outside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, const float* inside, float* outside, DevLive V,
+                   Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
   const Smem sm = carve(smem, L, chunk);
   float* P = sm.P;
   float* Q = sm.Q;
-  const SentCell sc = span_cell(B, span, blockIdx.x);
-  const int s = sc.s, b = sc.b, e = b + span, n = B.len[s];
+  const int ent = entry_of(W, blockIdx.x);
+  const int s = W.sent[ent], span = span_of(W, ent), b = (int)blockIdx.x - W.pref[ent], e = b + span, n = B.len[s];
   const long long off = B.cell_off[s], toff = off + tri(n);
   const long long cbot = off + chart_index(b, e, n), ctop = toff + chart_index(b, e, n);
   auto BOT = [&](int x, int y) { return off + chart_index(x, y, n); };
@@ -525,7 +527,7 @@ __global__ void __launch_bounds__(256) k_outside_span(DevLevel L, DevBatch B, De
   // unary layer: outside-bot from outside-top.  With a batch of one-word
   // sentences only, the reference's first unary call (at span == maxLength)
   // uses the nonterminal unaries and its span loop never runs.
-  const bool use_tu = span == 1 && B.max_len > 1;
+  const bool use_tu = span == 1 && !W.one_word_batch;
   const float us = S == SEMI_REAL ? __expf(-scale_of(OS, cbot) + scale_of(OS, ctop)) : 1.f;
   unary_into<S>(L.ujobs[use_tu ? OUT_TU : OUT_NU], P, Q, cs, X.flag0 != 0, us);
   __syncthreads();
@@ -565,17 +567,14 @@ __global__ void __launch_bounds__(256) k_outside_span(DevLevel L, DevBatch B, De
 // Lexicon (CLParser.scala:426-467): one warp per token writes its bot span-1
 // cell: the semiring zero except the word's allowed preterminals.
 template <int S>
-__global__ void k_lexicon(DevLevel L, DevBatch B, DevMask M, float* inside, double* part_scale, DevLive V,
-                          int* status) {
-  const long long tok = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+__global__ void k_lexicon(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, double* part_scale,
+                          DevLive V, int* status) {
+  const long long unit = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (tok >= B.num_tokens) return;
-  int lo = 0, hi = B.nsent;
-  while (hi - lo > 1) {
-    int mid = (lo + hi) >> 1;
-    if (B.word_off[mid] <= tok) lo = mid; else hi = mid;
-  }
-  const int s = lo, pos = (int)(tok - B.word_off[s]);
+  if (unit >= W.nunits) return;
+  const int ent = entry_of(W, (int)unit);
+  const int s = W.sent[ent], pos = (int)unit - W.pref[ent];
+  const long long tok = B.word_off[s] + pos;
   const int cs = L.cell_size, ms = L.mask_size;
   const long long cell = B.cell_off[s] + pos;  // chartIndex(pos, pos + 1) == pos
   float* row = inside + cell * cs;
@@ -647,15 +646,15 @@ int pick_split_chunk(int cell_size, int max_len) {
   return chunk;
 }
 
-cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevMask& M, float* inside,
+cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M, float* inside,
                            double* part_scale, DevLive V, Counters C, cudaStream_t st) {
-  const long long warps = B.num_tokens;
+  const long long warps = W.nunits;
   const int blocks = (int)((warps * 32 + 127) / 128);
   if (blocks == 0) return cudaSuccess;
   switch (L.semiring) {
-    case SEMI_VITERBI: k_lexicon<SEMI_VITERBI><<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, V, C.status); break;
-    case SEMI_REAL: k_lexicon<SEMI_REAL><<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, V, C.status); break;
-    default: k_lexicon<SEMI_LOGSUM><<<blocks, 128, 0, st>>>(L, B, M, inside, part_scale, V, C.status); break;
+    case SEMI_VITERBI: k_lexicon<SEMI_VITERBI><<<blocks, 128, 0, st>>>(L, B, W, M, inside, part_scale, V, C.status); break;
+    case SEMI_REAL: k_lexicon<SEMI_REAL><<<blocks, 128, 0, st>>>(L, B, W, M, inside, part_scale, V, C.status); break;
+    default: k_lexicon<SEMI_LOGSUM><<<blocks, 128, 0, st>>>(L, B, W, M, inside, part_scale, V, C.status); break;
   }
   return cudaGetLastError();
 }
@@ -663,46 +662,50 @@ cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevMask& 
 namespace {
 
 template <int S, int MODE>
-cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                        const float* inside_c, float* inside, float* outside, DevLive V, Counters C, cudaStream_t st) {
-  const int chunk = pick_split_chunk(L.cell_size, B.max_len);
+cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                        int max_span, const float* inside_c, float* inside, float* outside, DevLive V, Counters C,
+                        cudaStream_t st) {
+  const int chunk = pick_split_chunk(L.cell_size, max_span);
   const size_t smem = pass_smem_bytes(L, chunk);
+  const unsigned grid = (unsigned)W.nunits;
   if (inside_pass) {
     set_smem(k_inside_span<S, MODE>, smem);
-    k_inside_span<S, MODE><<<ncells, kThreads, smem, st>>>(L, B, M, span, inside, V, C, chunk);
+    k_inside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside, V, C, chunk);
   } else {
     set_smem(k_outside_span<S, MODE>, smem);
-    k_outside_span<S, MODE><<<ncells, kThreads, smem, st>>>(L, B, M, span, inside_c, outside, V, C, chunk);
+    k_outside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside_c, outside, V, C, chunk);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_any(bool inside_pass, const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                       const float* inside_c, float* inside, float* outside, DevLive V, Counters C, cudaStream_t st) {
-  if (ncells == 0) return cudaSuccess;
+cudaError_t launch_any(bool inside_pass, const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                       int max_span, const float* inside_c, float* inside, float* outside, DevLive V, Counters C,
+                       cudaStream_t st) {
+  if (W.nunits == 0) return cudaSuccess;
   const bool pairs = L.mode == 2;
   switch (L.semiring) {
     case SEMI_VITERBI:
-      return pairs ? launch_pass<SEMI_VITERBI, 2>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st)
-                   : launch_pass<SEMI_VITERBI, 0>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st);
+      return pairs ? launch_pass<SEMI_VITERBI, 2>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st)
+                   : launch_pass<SEMI_VITERBI, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
     case SEMI_REAL:
-      return pairs ? launch_pass<SEMI_REAL, 2>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st)
-                   : launch_pass<SEMI_REAL, 0>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st);
+      return pairs ? launch_pass<SEMI_REAL, 2>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st)
+                   : launch_pass<SEMI_REAL, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
     default:
-      return launch_pass<SEMI_LOGSUM, 0>(inside_pass, L, B, M, span, ncells, inside_c, inside, outside, V, C, st);
+      return launch_pass<SEMI_LOGSUM, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
   }
 }
 
 }  // namespace
 
-cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                               float* inside, DevLive V, Counters C, cudaStream_t st) {
-  return launch_any(true, L, B, M, span, ncells, inside, inside, nullptr, V, C, st);
+cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                               int max_span, float* inside, DevLive V, Counters C, cudaStream_t st) {
+  return launch_any(true, L, B, W, M, max_span, inside, inside, nullptr, V, C, st);
 }
 
-cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                                const float* inside, float* outside, DevLive V, Counters C, cudaStream_t st) {
-  return launch_any(false, L, B, M, span, ncells, inside, nullptr, outside, V, C, st);
+cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                                int max_span, const float* inside, float* outside, DevLive V, Counters C,
+                                cudaStream_t st) {
+  return launch_any(false, L, B, W, M, max_span, inside, nullptr, outside, V, C, st);
 }
 
 }  // namespace puck

@@ -72,23 +72,33 @@ struct DevLevel {
   const float* v_score;
 };
 
-// One batch of sentences laid out like the reference's Batch
-// (src/main/scala/puck/parser/Batch.scala:218-253): per sentence a bot half
-// then a top half of n(n+1)/2 cells each, cells in span-major chartIndex order.
+// Sentences of a batch (or of a server's resident set).  Each sentence's
+// chart is laid out like the reference's Batch (src/main/scala/puck/parser/
+// Batch.scala:218-253): a bot half then a top half of n(n+1)/2 cells each, in
+// span-major chartIndex order, starting at cell_off[s].  In batch mode the
+// sentences are packed back to back; a server places them anywhere in its
+// resident chart arena.
 struct DevBatch {
   int nsent;
-  int max_len;
-  long long num_cells;
-  long long num_tokens;
   const int* len;             // [nsent]
-  const long long* cell_off;  // [nsent + 1]
-  const long long* word_off;  // [nsent + 1]
-  const int* words;           // [num_tokens]
-  const int* order;           // sentence ids sorted by length, longest first
-  const int* span_pref;       // per span L: prefix sums of (len - L + 1) over order[0..k_L)
-  const int* span_base;       // [max_len + 2] offset of span L's prefix array
-  const int* span_count;      // [max_len + 2] k_L = number of sentences with len >= L
-  const long long* node_off;  // [nsent + 1] first tree node of each sentence
+  const long long* cell_off;  // [nsent] first cell of each sentence
+  const long long* word_off;  // [nsent] first word id of each sentence
+  const int* words;
+  const long long* node_off;  // [nsent] first tree node of each sentence
+};
+
+// The units of one launch: entries are sentences; unit i belongs to the entry
+// k with pref[k] <= i < pref[k+1].  Units are cells of one span length per
+// entry (span passes), tokens (lexicon), cells (per-cell kernels) or whole
+// sentences (decoders).  One launch can mix sentences at different spans.
+struct DevWork {
+  int nent;
+  long long nunits;         // pref[nent], kept on the host side for grid sizes
+  const int* sent;          // [nent] sentence index
+  const int* span;          // [nent] span length of the entry's cells; null: span_all for every entry
+  int span_all;
+  const int* pref;          // [nent + 1]; null for per-sentence launches (unit k is entry k)
+  int one_word_batch;       // outside pass: the reference's batch-of-one-word-sentences unary quirk
 };
 
 // Pruning mask and log-scales produced by the previous level.
@@ -115,23 +125,29 @@ struct DevLive {
   int* out;   // [num_cells * mask_size] outside chart (may be null)
 };
 
-cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevMask& M, float* inside,
+// Launch wrappers.  Every wrapper takes the host-side unit count of its work
+// list (W.nunits) as the grid size; part_scale and log_z are indexed by
+// sentence.
+cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M, float* inside,
                            double* part_scale, DevLive V, Counters C, cudaStream_t st);
-cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                               float* inside, DevLive V, Counters C, cudaStream_t st);
-cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevMask& M, int span, int ncells,
-                                const float* inside, float* outside, DevLive V, Counters C, cudaStream_t st);
-cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
-                         float thresh, int* masks_out, cudaStream_t st);
-cudaError_t launch_scaling(int cell_size, long long num_cells, const float* chart, float* out, cudaStream_t st);
-cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const float* inside, DevNode* nodes,
+cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                               int max_span, float* inside, DevLive V, Counters C, cudaStream_t st);
+cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                                int max_span, const float* inside, float* outside, DevLive V, Counters C,
+                                cudaStream_t st);
+cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const DevWork& W, const float* inside,
+                         const float* outside, float thresh, int* masks_out, cudaStream_t st);
+cudaError_t launch_scaling(int cell_size, const DevBatch& B, const DevWork& W, const float* chart, float* out,
                            cudaStream_t st);
-cudaError_t launch_mbr_cells(const DevLevel& L, const DevBatch& B, const float* inside, const float* outside,
-                             float2* decode, cudaStream_t st);
-cudaError_t launch_mbr_decode(const DevBatch& B, const DevMask& M, int scaling, const float2* decode,
-                              const long long* mbr_off, float* scratch, DevNode* nodes, cudaStream_t st);
-cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevMask& M, const float* inside,
-                               const double* part_scale, float* log_z, cudaStream_t st);
+cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const DevWork& W, int max_len, const float* inside,
+                           DevNode* nodes, cudaStream_t st);
+cudaError_t launch_mbr_cells(const DevLevel& L, const DevBatch& B, const DevWork& W, const float* inside,
+                             const float* outside, float2* decode, cudaStream_t st);
+cudaError_t launch_mbr_decode(const DevBatch& B, const DevWork& W, const DevMask& M, int scaling,
+                              const float2* decode, const long long* mbr_off, float* scratch, DevNode* nodes,
+                              cudaStream_t st);
+cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
+                               const float* inside, const double* part_scale, float* log_z, cudaStream_t st);
 
 size_t pass_smem_bytes(const DevLevel& L, int chunk);
 

@@ -10,8 +10,7 @@
 // (WorkSpace.getBatches, src/main/scala/puck/parser/WorkSpace.scala:20-41);
 // results do not depend on how sentences are batched.
 
-#include "puck_internal.h"
-#include "../../include/puck_gpu.h"
+#include "host_runtime.h"
 
 #include <algorithm>
 #include <array>
@@ -27,24 +26,14 @@
 #include <unordered_map>
 #include <vector>
 
+using namespace puck_host;
+
 namespace {
 
 thread_local std::string g_last_error;
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
-struct PuckError {
-  puck_status status;
-  std::string msg;
-};
-
-#define CUDA_TRY(expr)                                                                          \
-  do {                                                                                          \
-    cudaError_t _e = (expr);                                                                    \
-    if (_e != cudaSuccess)                                                                      \
-      throw PuckError{_e == cudaErrorMemoryAllocation ? PUCK_ERR_OOM : PUCK_ERR_CUDA,           \
-                      std::string(#expr) + ": " + cudaGetErrorString(_e)};                      \
-  } while (0)
 
 // ---------------------------------------------------------------------------
 // Minimal reader for zip archives with stored (uncompressed) entries.
@@ -96,26 +85,6 @@ struct ZipReader {
   }
 };
 
-struct Array {
-  char tag[5] = {0};
-  std::vector<char> bytes;
-  int64_t count = 0;
-};
-
-struct HostLevel {
-  int semiring = 0, n_nt = 0, n_t = 0, cell_size = 0, mask_size = 0, n_coarse = 0, root = 0, n_words = 0;
-  std::map<std::string, Array> arrays;
-  std::vector<std::string> words;
-
-  template <class T>
-  const T* get(const std::string& name, const char* tag, int64_t* count) const {
-    auto it = arrays.find(name);
-    if (it == arrays.end()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "missing array " + name};
-    if (std::strncmp(it->second.tag, tag, 2) != 0) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad dtype for " + name};
-    if (count) *count = it->second.count;
-    return reinterpret_cast<const T*>(it->second.bytes.data());
-  }
-};
 
 std::vector<std::string> split_lines(const std::string& s) {
   std::vector<std::string> out;
@@ -133,10 +102,6 @@ std::vector<std::string> split_lines(const std::string& s) {
 
 void puck::set_last_error(const char* msg) { set_error(msg); }
 
-struct puck_grammar {
-  std::vector<HostLevel> levels;
-  std::unordered_map<std::string, int> word_index;
-};
 
 namespace {
 
@@ -320,40 +285,7 @@ void load_grammar(puck_grammar* g, const std::string& path) {
 }
 
 // ---------------------------------------------------------------------------
-struct DevBuf {
-  void* p = nullptr;
-  size_t cap = 0;
-  void ensure(size_t bytes) {
-    if (bytes <= cap) return;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(bytes + bytes / 8, 256);
-    CUDA_TRY(cudaMalloc(&p, want));
-    cap = want;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T> T* as() const { return reinterpret_cast<T*>(p); }
-};
 
-struct LevelDev {
-  std::vector<void*> allocs;
-  puck::DevLevel d{};
-  void* upload(const void* src, size_t bytes) {
-    void* p = nullptr;
-    CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
-    allocs.push_back(p);
-    if (bytes) CUDA_TRY(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
-    return p;
-  }
-  ~LevelDev() {
-    for (void* p : allocs) cudaFree(p);
-  }
-};
 
 template <class T>
 const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char* tag, int64_t* count = nullptr) {
@@ -363,7 +295,9 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
   return reinterpret_cast<const T*>(D.upload(h, c * sizeof(T)));
 }
 
-void build_level(LevelDev& D, const HostLevel& L, bool merged) {
+}  // namespace
+
+void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
   puck::DevLevel& d = D.d;
   d.semiring = L.semiring;
   d.n_nt = L.n_nt;
@@ -458,6 +392,8 @@ void build_level(LevelDev& D, const HostLevel& L, bool merged) {
   d.v_score = up<float>(D, L, "v_score", "f4");
 }
 
+namespace {
+
 long long tri(int n) { return (long long)n * (n + 1) / 2; }
 
 enum Mode { MODE_PARSE = 0, MODE_PARTITIONS = 1, MODE_INSIDE_OUTSIDE = 2 };
@@ -474,7 +410,7 @@ struct puck_parser {
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<LevelDev>> levels;
   std::vector<LevelBufs> bufs;
-  DevBuf b_len, b_cell_off, b_word_off, b_words, b_order, b_span_pref, b_span_base, b_span_count, b_node_off,
+  DevBuf b_len, b_cell_off, b_word_off, b_words, b_work, b_node_off,
       b_mbr_off, b_nodes, b_status, b_logz, b_scratch, b_counters;
   puck::DevBatch last_batch{};
   int64_t last_num_cells = 0;
@@ -529,24 +465,35 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     mbr_off[i + 1] = mbr_off[i] + 3LL * (len[i] + 1) * (len[i] + 1);
     words.insert(words.end(), word_ids + offsets[s], word_ids + offsets[s + 1]);
   }
+  // Work lists, concatenated into one upload.  Span launches take the
+  // sentences that have cells of that span, longest first; the lexicon, the
+  // per-cell kernels and the per-sentence kernels take every sentence.
   std::vector<int> order(ns);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return len[a] > len[b]; });
-  std::vector<int> span_pref, span_base(max_len + 2, 0), span_count(max_len + 2, 0), span_cells(max_len + 2, 0);
+  std::vector<int> wl;
+  struct ListAt { size_t sent, pref; int nent; long long nunits; };
+  auto add_list = [&](int nent, auto sent_of, auto units_of) {
+    ListAt at{wl.size(), 0, nent, 0};
+    for (int k = 0; k < nent; ++k) wl.push_back(sent_of(k));
+    at.pref = wl.size();
+    long long acc = 0;
+    wl.push_back(0);
+    for (int k = 0; k < nent; ++k) {
+      acc += units_of(k);
+      wl.push_back((int)acc);
+    }
+    at.nunits = acc;
+    return at;
+  };
+  std::vector<ListAt> span_list(max_len + 1);
   for (int L = 1; L <= max_len; ++L) {
-    span_base[L] = (int)span_pref.size();
     int k = 0;
     while (k < ns && len[order[k]] >= L) ++k;
-    span_count[L] = k;
-    int acc = 0;
-    span_pref.push_back(0);
-    for (int j = 0; j < k; ++j) {
-      acc += len[order[j]] - L + 1;
-      span_pref.push_back(acc);
-    }
-    span_cells[L] = acc;
+    span_list[L] = add_list(k, [&](int j) { return order[j]; }, [&](int j) { return len[order[j]] - L + 1; });
   }
-  span_base[max_len + 1] = (int)span_pref.size();
+  const ListAt tok_list = add_list(ns, [](int j) { return j; }, [&](int j) { return len[j]; });
+  const ListAt cell_list = add_list(ns, [](int j) { return j; }, [&](int j) { return 2 * tri(len[j]); });
   const long long num_cells = cell_off[ns];
   auto h2d = [&](DevBuf& b, const void* src, size_t bytes) {
     b.ensure(std::max<size_t>(bytes, 16));
@@ -557,25 +504,31 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   h2d(P->b_cell_off, cell_off.data(), (ns + 1) * sizeof(long long));
   h2d(P->b_word_off, word_off.data(), (ns + 1) * sizeof(long long));
   h2d(P->b_words, words.data(), words.size() * sizeof(int));
-  h2d(P->b_order, order.data(), ns * sizeof(int));
-  h2d(P->b_span_pref, span_pref.data(), span_pref.size() * sizeof(int));
-  h2d(P->b_span_base, span_base.data(), span_base.size() * sizeof(int));
-  h2d(P->b_span_count, span_count.data(), span_count.size() * sizeof(int));
+  h2d(P->b_work, wl.data(), wl.size() * sizeof(int));
   h2d(P->b_node_off, node_off.data(), (ns + 1) * sizeof(long long));
   puck::DevBatch B{};
   B.nsent = ns;
-  B.max_len = max_len;
-  B.num_cells = num_cells;
-  B.num_tokens = word_off[ns];
   B.len = P->b_len.as<int>();
   B.cell_off = P->b_cell_off.as<long long>();
   B.word_off = P->b_word_off.as<long long>();
   B.words = P->b_words.as<int>();
-  B.order = P->b_order.as<int>();
-  B.span_pref = P->b_span_pref.as<int>();
-  B.span_base = P->b_span_base.as<int>();
-  B.span_count = P->b_span_count.as<int>();
   B.node_off = P->b_node_off.as<long long>();
+  const int* wdev = P->b_work.as<int>();
+  auto work = [&](const ListAt& a, int span) {
+    puck::DevWork W{};
+    W.nent = a.nent;
+    W.nunits = a.nunits;
+    W.sent = wdev + a.sent;
+    W.span = nullptr;
+    W.span_all = span;
+    W.pref = wdev + a.pref;
+    W.one_word_batch = max_len == 1;
+    return W;
+  };
+  const puck::DevWork Wtok = work(tok_list, 1), Wcell = work(cell_list, 0);
+  puck::DevWork Wsent = Wcell;
+  Wsent.pref = nullptr;
+  Wsent.nunits = ns;
   P->b_status.ensure(ns * sizeof(int) + 16);
   CUDA_TRY(cudaMemsetAsync(P->b_status.p, 0, ns * sizeof(int), st));
   P->b_counters.ensure(64);
@@ -608,30 +561,31 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     auto& EV = P->ev_level[l];
     auto& LC = launches_l[l];
     rec(EV[0]);
-    CUDA_TRY(puck::launch_lexicon(D, B, MM, inside, lb.part.as<double>(), V, C, st));
+    CUDA_TRY(puck::launch_lexicon(D, B, Wtok, MM, inside, lb.part.as<double>(), V, C, st));
     ++LC[0];
     for (int span = 1; span <= max_len; ++span) {
-      CUDA_TRY(puck::launch_inside_span(D, B, MM, span, span_cells[span], inside, V, C, st));
+      CUDA_TRY(puck::launch_inside_span(D, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
       ++LC[0];
     }
     rec(EV[1]);
     if (need_out) {
       for (int span = max_len; span >= 1; --span) {
-        CUDA_TRY(puck::launch_outside_span(D, B, MM, span, span_cells[span], inside, outside, V, C, st));
+        CUDA_TRY(puck::launch_outside_span(D, B, work(span_list[span], span), MM, max_len, inside, outside, V, C,
+                                           st));
         ++LC[1];
       }
     }
     rec(EV[2]);
     if (!last) {
       lb.masks.ensure(num_cells * D.mask_size * sizeof(int));
-      CUDA_TRY(puck::launch_masks(D, B, inside, outside, P->opt.prune_threshold, lb.masks.as<int>(), st));
+      CUDA_TRY(puck::launch_masks(D, B, Wcell, inside, outside, P->opt.prune_threshold, lb.masks.as<int>(), st));
       ++LC[2];
       lb.iscale.ensure(num_cells * sizeof(float));
       lb.oscale.ensure(num_cells * sizeof(float));
       const bool next_real = P->g->levels[l + 1].semiring == puck::SEMI_REAL;
       if (next_real) {
-        CUDA_TRY(puck::launch_scaling(D.cell_size, num_cells, inside, lb.iscale.as<float>(), st));
-        CUDA_TRY(puck::launch_scaling(D.cell_size, num_cells, outside, lb.oscale.as<float>(), st));
+        CUDA_TRY(puck::launch_scaling(D.cell_size, B, Wcell, inside, lb.iscale.as<float>(), st));
+        CUDA_TRY(puck::launch_scaling(D.cell_size, B, Wcell, outside, lb.oscale.as<float>(), st));
         LC[2] += 2;
       } else {
         CUDA_TRY(cudaMemsetAsync(lb.iscale.p, 0, num_cells * sizeof(float), st));
@@ -649,7 +603,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     rec(EV[3]);
     if (mode == MODE_PARTITIONS) {
       P->b_logz.ensure(ns * sizeof(float) + 16);
-      CUDA_TRY(puck::launch_root_scores(D, B, MM, inside, lb.part.as<double>(), P->b_logz.as<float>(), st));
+      CUDA_TRY(puck::launch_root_scores(D, B, Wsent, MM, inside, lb.part.as<double>(), P->b_logz.as<float>(), st));
       ++LC[3];
       rec(EV[4]);
       rec(P->ev_batch[1]);
@@ -665,17 +619,17 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
       if (vit) {
         if (D.semiring != puck::SEMI_VITERBI)
           throw PuckError{PUCK_ERR_INVALID_ARG, "Viterbi decoding needs a Viterbi fine level"};
-        CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
+        CUDA_TRY(puck::launch_viterbi(D, B, Wsent, max_len, inside, P->b_nodes.as<puck::DevNode>(), st));
         ++LC[3];
       } else {
         if (!M.bits) throw PuckError{PUCK_ERR_INVALID_ARG, "Can't use null pruning mask for parse extraction!"};
         if (D.semiring == puck::SEMI_VITERBI)
           throw PuckError{PUCK_ERR_INVALID_ARG, "MBR decoding needs a sum-product fine level"};
         lb.decode.ensure(num_cells * sizeof(float2));
-        CUDA_TRY(puck::launch_mbr_cells(D, B, inside, outside, lb.decode.as<float2>(), st));
+        CUDA_TRY(puck::launch_mbr_cells(D, B, Wcell, inside, outside, lb.decode.as<float2>(), st));
         h2d(P->b_mbr_off, mbr_off.data(), (ns + 1) * sizeof(long long));
         P->b_scratch.ensure(mbr_off[ns] * sizeof(float) + 16);
-        CUDA_TRY(puck::launch_mbr_decode(B, M, D.semiring == puck::SEMI_REAL ? 1 : 0, lb.decode.as<float2>(),
+        CUDA_TRY(puck::launch_mbr_decode(B, Wsent, M, D.semiring == puck::SEMI_REAL ? 1 : 0, lb.decode.as<float2>(),
                                          P->b_mbr_off.as<long long>(), P->b_scratch.as<float>(),
                                          P->b_nodes.as<puck::DevNode>(), st));
         LC[3] += 2;
@@ -695,10 +649,10 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
       // insideOutside: the decode kernels run, nothing is extracted (CLParser.scala:171-182)
       if (D.semiring == puck::SEMI_VITERBI) {
         P->b_nodes.ensure(node_off[ns] * sizeof(puck::DevNode) + 16);
-        CUDA_TRY(puck::launch_viterbi(D, B, inside, P->b_nodes.as<puck::DevNode>(), st));
+        CUDA_TRY(puck::launch_viterbi(D, B, Wsent, max_len, inside, P->b_nodes.as<puck::DevNode>(), st));
       } else {
         lb.decode.ensure(num_cells * sizeof(float2));
-        CUDA_TRY(puck::launch_mbr_cells(D, B, inside, outside, lb.decode.as<float2>(), st));
+        CUDA_TRY(puck::launch_mbr_cells(D, B, Wcell, inside, outside, lb.decode.as<float2>(), st));
       }
       ++LC[3];
       rec(EV[4]);
@@ -773,7 +727,9 @@ puck_status run_call(puck_parser* P, Mode mode, const int32_t* word_ids, const i
     if (log_z && mode == MODE_PARTITIONS)
       for (int s = 0; s < nsent; ++s) log_z[s] = std::nanf("");
     const int64_t per_cell = bytes_per_cell(P, mode);
-    const int64_t cap_cells = std::max<int64_t>(P->budget_bytes / std::max<int64_t>(per_cell, 1), 1);
+    // work-list prefixes are 32-bit: a batch holds fewer than 2^31 cells
+    const int64_t cap_cells = std::min<int64_t>(
+        std::max<int64_t>(P->budget_bytes / std::max<int64_t>(per_cell, 1), 1), (int64_t)INT32_MAX);
     std::vector<BatchPlan> plans;
     BatchPlan cur;
     int64_t cur_cells = 0;
@@ -912,8 +868,7 @@ void puck_parser_destroy(puck_parser* P) {
     b.inside.release(); b.outside.release(); b.masks.release(); b.iscale.release(); b.oscale.release();
     b.part.release(); b.decode.release(); b.live_in.release(); b.live_out.release();
   }
-  for (DevBuf* b : {&P->b_len, &P->b_cell_off, &P->b_word_off, &P->b_words, &P->b_order, &P->b_span_pref,
-                    &P->b_span_base, &P->b_span_count, &P->b_node_off, &P->b_mbr_off, &P->b_nodes, &P->b_status,
+  for (DevBuf* b : {&P->b_len, &P->b_cell_off, &P->b_word_off, &P->b_words, &P->b_work, &P->b_node_off, &P->b_mbr_off, &P->b_nodes, &P->b_status,
                     &P->b_logz, &P->b_scratch, &P->b_counters})
     b->release();
   P->levels.clear();

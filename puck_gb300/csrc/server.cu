@@ -1,0 +1,836 @@
+// Continuous-batching parse server (puck_server_* in puck_gpu.h).
+//
+// The reference batches parse requests in front of the parser:
+// BatchFunctionAnnotatorService (dlwh/puck, src/main/scala/puck/
+// AnnotatorService.scala:29-78) collects sentences until a time or size limit,
+// hands the batch to CLParser.parse and completes one future per sentence.
+// Here the request loop never waits for a batch to fill or drain:
+//
+//  * admission: a queued sentence is admitted as soon as a slot and a
+//    contiguous range of 2*n(n+1)/2 cells of the chart arena are free (first
+//    fit, FIFO order).  The arena holds every level's charts, liveness bits,
+//    pruning masks and scales for the admitted sentences; they stay resident
+//    until the sentence's tree is decoded.
+//  * ticks: every tick advances each resident sentence through its next pass
+//    steps (lexicon, inside span k, outside span k, masks, decode).  One
+//    kernel launch per step kind and level covers every sentence at that step,
+//    whatever its span length, through the work lists the pass kernels take.
+//    Launches of a tick run in the order lexicon, inside, outside, masks per
+//    level, then decode, so a sentence can take several consecutive steps in
+//    one tick (outside span 1, masks, next level's lexicon and inside span 1).
+//  * pipelining: the host prepares tick t+1 while the GPU runs tick t; the
+//    staging buffers and the tree output buffers are double-buffered.  A
+//    finished sentence's cells and slot are reused by sentences admitted in
+//    later ticks, which the single stream orders after its last kernel.
+//  * results: decoded trees are written by the decode kernels straight into
+//    mapped pinned host memory; the host hands them out once the tick's event
+//    has completed.
+//
+// Every kernel computes a cell from that sentence's own cells only, so a
+// result does not depend on which other sentences were resident with it.
+
+#include "host_runtime.h"
+
+#include <chrono>
+#include <climits>
+#include <condition_variable>
+#include <deque>
+#include <mutex>
+#include <numeric>
+#include <thread>
+
+using namespace puck_host;
+
+namespace {
+
+constexpr int kMaxLevels = 8;
+constexpr int kDefaultSlots = 65536;
+
+long long tri(long long n) { return n * (n + 1) / 2; }
+
+int64_t now_ns() {
+  return std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// Per-slot metadata written at the start of a tick.
+struct SlotUpdate {
+  long long cell_off, node_off, mbr_off;
+  int slot, len, words_at, fresh;
+};
+
+struct SlotTables {
+  int* len;
+  long long* cell_off;
+  long long* node_off;
+  long long* mbr_off;
+  int* words;
+  int* status;
+  double* part[kMaxLevels];
+  int nlevels;
+};
+
+__global__ void k_slot_update(SlotTables T, const SlotUpdate* U, const int* staged_words) {
+  const SlotUpdate u = U[blockIdx.x];
+  if (threadIdx.x == 0) {
+    T.len[u.slot] = u.len;
+    T.cell_off[u.slot] = u.cell_off;
+    T.node_off[u.slot] = u.node_off;
+    T.mbr_off[u.slot] = u.mbr_off;
+    if (u.fresh) {
+      T.status[u.slot] = 0;
+      for (int l = 0; l < T.nlevels; ++l)
+        if (T.part[l]) T.part[l][u.slot] = 0.0;
+    }
+  }
+  if (u.words_at >= 0)  // words live at the sentence's first cell index
+    for (int i = threadIdx.x; i < u.len; i += blockDim.x) T.words[u.cell_off + i] = staged_words[u.words_at + i];
+}
+
+// First-fit allocator of contiguous cell ranges.
+class CellArena {
+ public:
+  void init(long long cap) {
+    free_.clear();
+    free_[0] = cap;
+    cap_ = cap;
+    used_ = peak_ = 0;
+  }
+  long long alloc(long long n) {
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second < n) continue;
+      const long long off = it->first, rest = it->second - n;
+      free_.erase(it);
+      if (rest) free_[off + n] = rest;
+      used_ += n;
+      peak_ = std::max(peak_, used_);
+      return off;
+    }
+    return -1;
+  }
+  void release(long long off, long long n) {
+    used_ -= n;
+    auto next = free_.lower_bound(off);
+    if (next != free_.end() && next->first == off + n) {
+      n += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == off) {
+        prev->second += n;
+        return;
+      }
+    }
+    free_[off] = n;
+  }
+  long long cap() const { return cap_; }
+  long long peak() const { return peak_; }
+
+ private:
+  std::map<long long, long long> free_;
+  long long cap_ = 0, used_ = 0, peak_ = 0;
+};
+
+struct Request {
+  int n = 0;
+  int status = PUCK_OK;
+  int64_t t_arrival = 0, t_done = 0;
+  std::vector<int> words;
+  std::vector<puck_tree_node> nodes;
+};
+
+enum Stage { ST_LEX = 0, ST_IN = 1, ST_OUT = 2, ST_MASK = 3, ST_DEC = 4 };
+
+// A resident sentence and its pass cursor (owned by the loop thread).
+struct Resident {
+  int64_t id;
+  int slot, n;
+  long long cell_off;
+  int level, stage, span;
+  int upd;  // index of this tick's admission record, -1 after the admitting tick
+};
+
+struct Finishing {
+  int64_t id;
+  long long node_at;
+  int n;
+};
+
+// Host and device buffers of one tick in flight.
+struct TickBuf {
+  char* host = nullptr;  // pinned staging
+  size_t host_cap = 0;
+  DevBuf dev;
+  puck_tree_node* out_host = nullptr;  // mapped pinned tree output
+  puck::DevNode* out_dev = nullptr;
+  size_t out_cap = 0;  // nodes
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  std::vector<Finishing> finishing;
+  int64_t launches = 0, h2d = 0, d2h = 0;
+};
+
+struct LevelArena {
+  DevBuf inside, outside, live_in, live_out, masks, iscale, oscale, part;
+  bool need_out = false, next_real = false, last = false;
+};
+
+// One step list of a tick: entries (slot, span) and the unit prefix.
+struct StepList {
+  std::vector<int> sent, span, pref;
+  long long units = 0;
+  size_t at_sent = 0, at_span = 0, at_pref = 0;  // byte offsets in the staging buffer
+  void clear() {
+    sent.clear();
+    span.clear();
+    pref.clear();
+    units = 0;
+  }
+};
+
+}  // namespace
+
+struct puck_server {
+  const puck_grammar* g = nullptr;
+  puck_options opt{};
+  int nl = 0;
+  bool mbr = false;
+  cudaStream_t stream = nullptr;
+  std::vector<std::unique_ptr<LevelDev>> levels;
+  std::vector<LevelArena> la;
+  DevBuf d_len, d_cell_off, d_node_off, d_mbr_off, d_words, d_status, d_counters, d_decode, d_scratch;
+  int slots = 0;
+  CellArena arena;
+  std::vector<int> free_slots;
+  TickBuf tb[2];
+  std::vector<Resident> resident;  // loop thread only
+  std::vector<StepList> lists;     // loop thread only
+
+  mutable std::mutex mu;
+  std::condition_variable cv_submit, cv_done;
+  std::deque<int64_t> pending;
+  std::unordered_map<int64_t, Request> reqs;
+  std::deque<int64_t> done_q;
+  int64_t next_id = 0;
+  bool stopping = false;
+  puck_server_stats stats{};
+  std::thread loop;
+};
+
+namespace {
+
+void ensure_host(char*& p, size_t& cap, size_t bytes) {
+  if (bytes <= cap) return;
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  const size_t want = std::max<size_t>(bytes + bytes / 2, 1 << 20);
+  CUDA_TRY(cudaHostAlloc(reinterpret_cast<void**>(&p), want, cudaHostAllocDefault));
+  cap = want;
+}
+
+void ensure_out(TickBuf& T, size_t nodes) {
+  if (nodes <= T.out_cap) return;
+  if (T.out_host) cudaFreeHost(T.out_host);
+  T.out_host = nullptr;
+  T.out_dev = nullptr;
+  T.out_cap = 0;
+  const size_t want = std::max<size_t>(nodes + nodes / 2, 1 << 16);
+  void* h = nullptr;
+  CUDA_TRY(cudaHostAlloc(&h, want * sizeof(puck_tree_node), cudaHostAllocMapped));
+  void* d = nullptr;
+  CUDA_TRY(cudaHostGetDevicePointer(&d, h, 0));
+  T.out_host = static_cast<puck_tree_node*>(h);
+  T.out_dev = static_cast<puck::DevNode*>(d);
+  T.out_cap = want;
+}
+
+int group_of(const puck_server* S, const Resident& r) {
+  return r.stage == ST_DEC ? 4 * S->nl : 4 * r.level + r.stage;
+}
+
+long long units_of(const Resident& r) {
+  switch (r.stage) {
+    case ST_LEX: return r.n;
+    case ST_IN:
+    case ST_OUT: return r.n - r.span + 1;
+    default: return 2 * tri(r.n);
+  }
+}
+
+// Next pass step of a sentence (the order of CLParser.parse for one sentence:
+// per level lexicon, inside spans 1..n, outside spans n..1 where needed,
+// masks; then the decode of the last level).
+void advance(const puck_server* S, Resident& r) {
+  const LevelArena& A = S->la[r.level];
+  switch (r.stage) {
+    case ST_LEX: r.stage = ST_IN; r.span = 1; return;
+    case ST_IN:
+      if (r.span < r.n) { ++r.span; return; }
+      if (A.need_out) { r.stage = ST_OUT; r.span = r.n; return; }
+      r.stage = A.last ? ST_DEC : ST_MASK;
+      return;
+    case ST_OUT:
+      if (r.span > 1) { --r.span; return; }
+      r.stage = A.last ? ST_DEC : ST_MASK;
+      return;
+    case ST_MASK: ++r.level; r.stage = ST_LEX; r.span = 0; return;
+    default: return;
+  }
+}
+
+void fail_all(puck_server* S, puck_status st) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->stopping = true;  // the request loop has ended: later submits are refused
+  const int64_t t = now_ns();
+  auto fail = [&](int64_t id) {
+    Request& r = S->reqs[id];
+    r.status = st;
+    r.t_done = t;
+    S->done_q.push_back(id);
+    ++S->stats.failed;
+    ++S->stats.completed;
+  };
+  for (int64_t id : S->pending) fail(id);
+  S->pending.clear();
+  for (const Resident& r : S->resident) fail(r.id);
+  for (TickBuf& T : S->tb) {
+    for (const Finishing& f : T.finishing) fail(f.id);
+    T.finishing.clear();
+  }
+  S->resident.clear();
+  S->stats.resident = 0;
+  S->cv_done.notify_all();
+}
+
+void harvest(puck_server* S, int p) {
+  TickBuf& T = S->tb[p];
+  CUDA_TRY(cudaEventSynchronize(T.ev_end));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, T.ev_begin, T.ev_end));
+  const int64_t t = now_ns();
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (const Finishing& f : T.finishing) {
+    Request& r = S->reqs[f.id];
+    r.nodes.assign(T.out_host + f.node_at, T.out_host + f.node_at + (2 * f.n - 1));
+    r.t_done = t;
+    S->done_q.push_back(f.id);
+    ++S->stats.completed;
+  }
+  S->stats.ms_device += ms;
+  S->stats.kernel_launches += T.launches;
+  S->stats.h2d_bytes += T.h2d;
+  S->stats.d2h_bytes += T.d2h;
+  T.finishing.clear();
+  S->cv_done.notify_all();
+}
+
+// Builds, uploads and launches one tick into buffer p.  Returns false when
+// nothing was resident.
+bool run_tick(puck_server* S, int p) {
+  TickBuf& T = S->tb[p];
+  T.launches = T.h2d = T.d2h = 0;
+  std::vector<SlotUpdate> upd;
+  std::vector<int> staged_words;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    while (!S->pending.empty() && !S->free_slots.empty()) {
+      const int64_t id = S->pending.front();
+      Request& q = S->reqs[id];
+      const long long off = S->arena.alloc(2 * tri(q.n));
+      if (off < 0) break;
+      const int slot = S->free_slots.back();
+      S->free_slots.pop_back();
+      S->resident.push_back(Resident{id, slot, q.n, off, 0, ST_LEX, 0, (int)upd.size()});
+      upd.push_back(SlotUpdate{off, 0, 6 * off, slot, q.n, (int)staged_words.size(), 1});
+      staged_words.insert(staged_words.end(), q.words.begin(), q.words.end());
+      std::vector<int>().swap(q.words);
+      S->pending.pop_front();
+    }
+    S->stats.resident = (int64_t)S->resident.size();
+    S->stats.resident_peak = std::max(S->stats.resident_peak, S->stats.resident);
+    S->stats.arena_cells_peak = S->arena.peak();
+  }
+  if (S->resident.empty()) return false;
+
+  // step lists: each sentence takes its next steps while their launch comes
+  // later in the tick than the step it took before
+  const int G = 4 * S->nl + 1;
+  auto& lists = S->lists;
+  lists.resize(G);
+  for (auto& L : lists) L.clear();
+  std::vector<std::vector<std::pair<int, int>>> spans(G);  // (span, slot) for span-ordered lists
+  long long out_nodes = 0;
+  std::vector<Resident> keep;
+  keep.reserve(S->resident.size());
+  std::vector<std::pair<long long, long long>> freed_cells;
+  std::vector<int> freed_slots;
+  for (Resident r : S->resident) {
+    int last_g = -1;
+    bool done = false;
+    while (true) {
+      const int g = group_of(S, r);
+      if (g <= last_g) break;
+      StepList& L = lists[g];
+      L.sent.push_back(r.slot);
+      if (r.stage == ST_IN || r.stage == ST_OUT) L.span.push_back(r.span);
+      L.pref.push_back((int)units_of(r));  // per-entry units; prefix formed below
+      last_g = g;
+      if (r.stage == ST_DEC) {
+        T.finishing.push_back(Finishing{r.id, out_nodes, r.n});
+        // a sentence admitted in this tick keeps one record (two records of
+        // one slot would race in k_slot_update)
+        if (r.upd >= 0) upd[r.upd].node_off = out_nodes;
+        else upd.push_back(SlotUpdate{r.cell_off, out_nodes, 6 * r.cell_off, r.slot, r.n, -1, 0});
+        out_nodes += 2 * r.n - 1;
+        freed_cells.emplace_back(r.cell_off, 2 * tri(r.n));
+        freed_slots.push_back(r.slot);
+        done = true;
+        break;
+      }
+      advance(S, r);
+    }
+    r.upd = -1;
+    if (!done) keep.push_back(r);
+  }
+  S->resident.swap(keep);
+  // span lists longest span first (their CTAs run longest)
+  for (int g = 0; g < G; ++g) {
+    StepList& L = lists[g];
+    if (L.span.empty()) continue;
+    std::vector<int> idx(L.sent.size());
+    std::iota(idx.begin(), idx.end(), 0);
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return L.span[a] > L.span[b]; });
+    std::vector<int> s2(idx.size()), p2(idx.size()), u2(idx.size());
+    for (size_t k = 0; k < idx.size(); ++k) {
+      s2[k] = L.sent[idx[k]];
+      p2[k] = L.span[idx[k]];
+      u2[k] = L.pref[idx[k]];
+    }
+    L.sent.swap(s2);
+    L.span.swap(p2);
+    L.pref.swap(u2);
+  }
+  for (auto& L : lists) {
+    long long acc = 0;
+    std::vector<int> pref(L.pref.size() + 1, 0);
+    for (size_t k = 0; k < L.pref.size(); ++k) {
+      acc += L.pref[k];
+      if (acc > INT32_MAX) throw PuckError{PUCK_ERR_INTERNAL, "tick work list above 2^31 units"};
+      pref[k + 1] = (int)acc;
+    }
+    L.pref.swap(pref);
+    L.units = acc;
+  }
+
+  // staging layout: updates | words | per list sent, span, pref (16-byte aligned sections)
+  size_t bytes = 0;
+  auto section = [&](size_t n) {
+    const size_t at = bytes;
+    bytes += (n + 15) & ~size_t(15);
+    return at;
+  };
+  const size_t at_upd = section(upd.size() * sizeof(SlotUpdate));
+  const size_t at_words = section(staged_words.size() * sizeof(int));
+  for (auto& L : lists) {
+    L.at_sent = section(L.sent.size() * sizeof(int));
+    L.at_span = section(L.span.size() * sizeof(int));
+    L.at_pref = section(L.pref.size() * sizeof(int));
+  }
+  ensure_host(T.host, T.host_cap, bytes);
+  std::memcpy(T.host + at_upd, upd.data(), upd.size() * sizeof(SlotUpdate));
+  std::memcpy(T.host + at_words, staged_words.data(), staged_words.size() * sizeof(int));
+  for (auto& L : lists) {
+    std::memcpy(T.host + L.at_sent, L.sent.data(), L.sent.size() * sizeof(int));
+    std::memcpy(T.host + L.at_span, L.span.data(), L.span.size() * sizeof(int));
+    std::memcpy(T.host + L.at_pref, L.pref.data(), L.pref.size() * sizeof(int));
+  }
+  T.dev.ensure(std::max<size_t>(bytes, 16));
+  ensure_out(T, (size_t)out_nodes);
+  cudaStream_t st = S->stream;
+  CUDA_TRY(cudaEventRecord(T.ev_begin, st));
+  CUDA_TRY(cudaMemcpyAsync(T.dev.p, T.host, bytes, cudaMemcpyHostToDevice, st));
+  T.h2d = (int64_t)bytes;
+  T.d2h = out_nodes * (int64_t)sizeof(puck_tree_node);
+  const char* dbase = static_cast<const char*>(T.dev.p);
+  if (!upd.empty()) {
+    SlotTables tab{};
+    tab.len = S->d_len.as<int>();
+    tab.cell_off = S->d_cell_off.as<long long>();
+    tab.node_off = S->d_node_off.as<long long>();
+    tab.mbr_off = S->d_mbr_off.as<long long>();
+    tab.words = S->d_words.as<int>();
+    tab.status = S->d_status.as<int>();
+    tab.nlevels = S->nl;
+    for (int l = 0; l < S->nl; ++l) tab.part[l] = S->la[l].part.as<double>();
+    k_slot_update<<<(unsigned)upd.size(), 128, 0, st>>>(tab, reinterpret_cast<const SlotUpdate*>(dbase + at_upd),
+                                                        reinterpret_cast<const int*>(dbase + at_words));
+    CUDA_TRY(cudaGetLastError());
+    ++T.launches;
+  }
+  // freed ranges and slots become available to sentences admitted next tick
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (auto& c : freed_cells) S->arena.release(c.first, c.second);
+    for (int s : freed_slots) S->free_slots.push_back(s);
+  }
+
+  puck::DevBatch B{};
+  B.nsent = S->slots;
+  B.len = S->d_len.as<int>();
+  B.cell_off = S->d_cell_off.as<long long>();
+  B.word_off = S->d_cell_off.as<long long>();
+  B.words = S->d_words.as<int>();
+  B.node_off = S->d_node_off.as<long long>();
+  puck::Counters C{S->d_counters.as<unsigned long long>(), S->d_counters.as<unsigned long long>() + 1,
+                   S->d_status.as<int>()};
+  auto work = [&](const StepList& L) {
+    puck::DevWork W{};
+    W.nent = (int)L.sent.size();
+    W.nunits = L.units;
+    W.sent = reinterpret_cast<const int*>(dbase + L.at_sent);
+    W.span = L.span.empty() ? nullptr : reinterpret_cast<const int*>(dbase + L.at_span);
+    W.span_all = 0;
+    W.pref = reinterpret_cast<const int*>(dbase + L.at_pref);
+    W.one_word_batch = 0;
+    return W;
+  };
+  const int maxlen = S->opt.max_length;
+  puck::DevMask M{nullptr, 0, nullptr, nullptr};
+  for (int l = 0; l < S->nl; ++l) {
+    const puck::DevLevel& D = S->levels[l]->d;
+    LevelArena& A = S->la[l];
+    float* inside = A.inside.as<float>();
+    float* outside = A.need_out ? A.outside.as<float>() : nullptr;
+    const puck::DevLive V{A.live_in.as<int>(), A.need_out ? A.live_out.as<int>() : nullptr};
+    puck::DevMask MM = M;
+    if (D.semiring != puck::SEMI_REAL) { MM.iscale = nullptr; MM.oscale = nullptr; }
+    const StepList& Llex = lists[4 * l + ST_LEX];
+    const StepList& Lin = lists[4 * l + ST_IN];
+    const StepList& Lout = lists[4 * l + ST_OUT];
+    const StepList& Lmask = lists[4 * l + ST_MASK];
+    if (!Llex.sent.empty()) {
+      CUDA_TRY(puck::launch_lexicon(D, B, work(Llex), MM, inside, A.part.as<double>(), V, C, st));
+      ++T.launches;
+    }
+    if (!Lin.sent.empty()) {
+      CUDA_TRY(puck::launch_inside_span(D, B, work(Lin), MM, maxlen, inside, V, C, st));
+      ++T.launches;
+    }
+    if (!Lout.sent.empty()) {
+      CUDA_TRY(puck::launch_outside_span(D, B, work(Lout), MM, maxlen, inside, outside, V, C, st));
+      ++T.launches;
+    }
+    if (!A.last) {
+      if (!Lmask.sent.empty()) {
+        const puck::DevWork W = work(Lmask);
+        CUDA_TRY(puck::launch_masks(D, B, W, inside, outside, S->opt.prune_threshold, A.masks.as<int>(), st));
+        ++T.launches;
+        if (A.next_real) {
+          CUDA_TRY(puck::launch_scaling(D.cell_size, B, W, inside, A.iscale.as<float>(), st));
+          CUDA_TRY(puck::launch_scaling(D.cell_size, B, W, outside, A.oscale.as<float>(), st));
+          T.launches += 2;
+        }
+      }
+      M.bits = A.masks.as<int>();
+      M.mask_size = D.mask_size;
+      M.iscale = A.next_real ? A.iscale.as<float>() : nullptr;
+      M.oscale = A.next_real ? A.oscale.as<float>() : nullptr;
+      continue;
+    }
+    const StepList& Ldec = lists[4 * S->nl];
+    if (Ldec.sent.empty()) continue;
+    puck::DevWork W = work(Ldec);
+    if (!S->mbr) {
+      CUDA_TRY(puck::launch_viterbi(D, B, W, maxlen, inside, T.out_dev, st));
+      ++T.launches;
+    } else {
+      CUDA_TRY(puck::launch_mbr_cells(D, B, W, inside, outside, S->d_decode.as<float2>(), st));
+      W.pref = nullptr;
+      CUDA_TRY(puck::launch_mbr_decode(B, W, M, D.semiring == puck::SEMI_REAL ? 1 : 0, S->d_decode.as<float2>(),
+                                       S->d_mbr_off.as<long long>(), S->d_scratch.as<float>(), T.out_dev, st));
+      T.launches += 2;
+    }
+  }
+  CUDA_TRY(cudaEventRecord(T.ev_end, st));
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    ++S->stats.ticks;
+    S->stats.resident = (int64_t)S->resident.size();
+  }
+  return true;
+}
+
+void loop_main(puck_server* S) {
+  try {
+    CUDA_TRY(cudaSetDevice(S->opt.device));
+    std::deque<int> inflight;
+    uint64_t tick = 0;
+    while (true) {
+      bool idle;
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        idle = S->resident.empty() && inflight.empty();
+        if (idle) {
+          S->cv_submit.wait(lk, [&] { return S->stopping || !S->pending.empty(); });
+          if (S->pending.empty()) break;  // stopping with nothing left
+        }
+      }
+      if (inflight.size() >= 2) {
+        harvest(S, inflight.front());
+        inflight.pop_front();
+      }
+      const int p = (int)(tick & 1);
+      if (run_tick(S, p)) {
+        inflight.push_back(p);
+        ++tick;
+      } else if (!inflight.empty()) {
+        harvest(S, inflight.front());
+        inflight.pop_front();
+      } else {
+        // nothing resident and nothing admissible: wait for a submit
+        std::unique_lock<std::mutex> lk(S->mu);
+        S->cv_submit.wait_for(lk, std::chrono::milliseconds(1));
+      }
+    }
+  } catch (const PuckError& e) {
+    puck::set_last_error(e.msg);
+    fail_all(S, e.status);
+  }
+}
+
+int64_t server_bytes_per_cell(const puck_server* S) {
+  int64_t b = 4;  // the sentence's words at its first cells
+  for (int l = 0; l < S->nl; ++l) {
+    const HostLevel& L = S->g->levels[l];
+    const LevelArena& A = S->la[l];
+    const int k = A.need_out ? 2 : 1;
+    b += (int64_t)(L.cell_size + L.mask_size) * 4 * k;
+    if (!A.last) b += (int64_t)L.mask_size * 4;
+    if (A.next_real) b += 8;
+  }
+  if (S->mbr) b += 8 + 24;  // per-cell decode pairs; decode tables (3(n+1)^2 <= 6 n(n+1) floats)
+  return b;
+}
+
+void destroy_server(puck_server* S) {
+  cudaSetDevice(S->opt.device);
+  for (TickBuf& T : S->tb) {
+    if (T.host) cudaFreeHost(T.host);
+    if (T.out_host) cudaFreeHost(T.out_host);
+    T.dev.release();
+    if (T.ev_begin) cudaEventDestroy(T.ev_begin);
+    if (T.ev_end) cudaEventDestroy(T.ev_end);
+  }
+  for (LevelArena& A : S->la)
+    for (DevBuf* b : {&A.inside, &A.outside, &A.live_in, &A.live_out, &A.masks, &A.iscale, &A.oscale, &A.part})
+      b->release();
+  for (DevBuf* b : {&S->d_len, &S->d_cell_off, &S->d_node_off, &S->d_mbr_off, &S->d_words, &S->d_status,
+                    &S->d_counters, &S->d_decode, &S->d_scratch})
+    b->release();
+  S->levels.clear();
+  if (S->stream) cudaStreamDestroy(S->stream);
+  delete S;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t puck_server_now_ns(void) { return now_ns(); }
+
+puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts, puck_status* status) {
+  auto* S = new puck_server();
+  try {
+    if (!g) throw PuckError{PUCK_ERR_INVALID_ARG, "null grammar"};
+    S->g = g;
+    if (opts) S->opt = *opts;
+    else puck_default_options(&S->opt);
+    if (S->opt.max_length <= 0) S->opt.max_length = 100;
+    if (S->opt.max_length > puck::kMaxLen)
+      throw PuckError{PUCK_ERR_INVALID_ARG, "max_length above " + std::to_string(puck::kMaxLen)};
+    S->nl = (int)g->levels.size();
+    if (S->nl < 1 || S->nl > kMaxLevels) throw PuckError{PUCK_ERR_INVALID_ARG, "unsupported number of levels"};
+    const HostLevel& fine = g->levels.back();
+    const bool vit = S->opt.decode == PUCK_DECODE_VITERBI ||
+                     (S->opt.decode == PUCK_DECODE_AUTO && fine.semiring == puck::SEMI_VITERBI);
+    if (vit && fine.semiring != puck::SEMI_VITERBI)
+      throw PuckError{PUCK_ERR_INVALID_ARG, "Viterbi decoding needs a Viterbi fine level"};
+    if (!vit && fine.semiring == puck::SEMI_VITERBI)
+      throw PuckError{PUCK_ERR_INVALID_ARG, "MBR decoding needs a sum-product fine level"};
+    if (!vit && S->nl < 2) throw PuckError{PUCK_ERR_INVALID_ARG, "Can't use null pruning mask for parse extraction!"};
+    S->mbr = !vit;
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (S->opt.device < 0 || S->opt.device >= ndev) throw PuckError{PUCK_ERR_INVALID_ARG, "no such CUDA device"};
+    CUDA_TRY(cudaSetDevice(S->opt.device));
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    for (TickBuf& T : S->tb) {
+      CUDA_TRY(cudaEventCreate(&T.ev_begin));
+      CUDA_TRY(cudaEventCreate(&T.ev_end));
+    }
+    for (int l = 0; l < S->nl; ++l) {
+      S->levels.emplace_back(new LevelDev());
+      build_level(*S->levels.back(), g->levels[l], l < S->nl - 1 && S->nl != 1);
+    }
+    S->la.resize(S->nl);
+    for (int l = 0; l < S->nl; ++l) {
+      LevelArena& A = S->la[l];
+      A.last = l == S->nl - 1;
+      A.need_out = !A.last || S->mbr;
+      A.next_real = !A.last && g->levels[l + 1].semiring == puck::SEMI_REAL;
+    }
+    S->slots = S->opt.max_batch_sentences > 0 ? S->opt.max_batch_sentences : kDefaultSlots;
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t cap = (int64_t)(free_b * 0.8);
+    const int64_t budget = S->opt.mem_bytes > 0 ? std::min<int64_t>(S->opt.mem_bytes, cap) : cap;
+    const int64_t per_slot = 4 + 8 * 3 + 4 + 8 * S->nl;
+    const int64_t per_cell = server_bytes_per_cell(S);
+    const int64_t cells = std::min<int64_t>((budget - per_slot * S->slots) / per_cell, (int64_t)INT32_MAX - 1);
+    if (cells < 2 * tri(S->opt.max_length))
+      throw PuckError{PUCK_ERR_OOM, "memory budget holds no sentence of the maximum length"};
+    S->arena.init(cells);
+    for (int l = 0; l < S->nl; ++l) {
+      const HostLevel& L = g->levels[l];
+      LevelArena& A = S->la[l];
+      A.inside.ensure(cells * L.cell_size * sizeof(float));
+      A.live_in.ensure(cells * L.mask_size * sizeof(int));
+      if (A.need_out) {
+        A.outside.ensure(cells * L.cell_size * sizeof(float));
+        A.live_out.ensure(cells * L.mask_size * sizeof(int));
+      }
+      if (!A.last) A.masks.ensure(cells * L.mask_size * sizeof(int));
+      if (A.next_real) {
+        A.iscale.ensure(cells * sizeof(float));
+        A.oscale.ensure(cells * sizeof(float));
+      }
+      A.part.ensure(S->slots * sizeof(double));
+    }
+    S->d_len.ensure(S->slots * sizeof(int));
+    S->d_cell_off.ensure(S->slots * sizeof(long long));
+    S->d_node_off.ensure(S->slots * sizeof(long long));
+    S->d_mbr_off.ensure(S->slots * sizeof(long long));
+    S->d_status.ensure(S->slots * sizeof(int));
+    S->d_words.ensure(cells * sizeof(int));
+    S->d_counters.ensure(64);
+    CUDA_TRY(cudaMemsetAsync(S->d_counters.p, 0, 64, S->stream));
+    if (S->mbr) {
+      S->d_decode.ensure(cells * sizeof(float2));
+      S->d_scratch.ensure(6 * cells * sizeof(float));
+    }
+    CUDA_TRY(cudaStreamSynchronize(S->stream));
+    S->free_slots.resize(S->slots);
+    for (int i = 0; i < S->slots; ++i) S->free_slots[i] = S->slots - 1 - i;
+    S->stats.arena_cells = cells;
+    S->loop = std::thread(loop_main, S);
+    if (status) *status = PUCK_OK;
+    return S;
+  } catch (const PuckError& e) {
+    puck::set_last_error(e.msg);
+    if (status) *status = e.status;
+  }
+  destroy_server(S);
+  return nullptr;
+}
+
+void puck_server_destroy(puck_server* S) {
+  if (!S) return;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stopping = true;
+  }
+  S->cv_submit.notify_all();
+  if (S->loop.joinable()) S->loop.join();
+  destroy_server(S);
+}
+
+puck_status puck_server_submit(puck_server* S, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                               const int64_t* arrival_ns, int64_t* ids) {
+  if (!S || nsent < 0 || (nsent > 0 && (!word_ids || !offsets || !ids))) {
+    puck::set_last_error("puck_server_submit: null argument or negative count");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  const int64_t t = now_ns();
+  const int nwords = S->g->levels.back().n_words;
+  const long long cap = S->arena.cap();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (S->stopping) {
+      puck::set_last_error("puck_server_submit: server is stopping");
+      return PUCK_ERR_INVALID_ARG;
+    }
+    for (int i = 0; i < nsent; ++i) {
+      const int64_t id = S->next_id++;
+      Request& r = S->reqs[id];
+      const int64_t n = offsets[i + 1] - offsets[i];
+      r.n = (int)std::max<int64_t>(n, 0);
+      r.t_arrival = arrival_ns && arrival_ns[i] > 0 ? arrival_ns[i] : t;
+      int st = PUCK_OK;
+      if (n <= 0) st = PUCK_ERR_EMPTY;
+      else if (n > S->opt.max_length) st = PUCK_ERR_SENT_TOO_LONG;
+      else if (2 * tri(n) > cap) st = PUCK_ERR_OOM;
+      else
+        for (int64_t k = offsets[i]; k < offsets[i + 1]; ++k)
+          if (word_ids[k] < 0 || word_ids[k] >= nwords) { st = PUCK_ERR_OOV; break; }
+      ids[i] = id;
+      ++S->stats.submitted;
+      if (st != PUCK_OK) {
+        r.status = st;
+        r.t_done = t;
+        S->done_q.push_back(id);
+        ++S->stats.completed;
+        ++S->stats.failed;
+        continue;
+      }
+      r.words.assign(word_ids + offsets[i], word_ids + offsets[i + 1]);
+      S->pending.push_back(id);
+    }
+  }
+  S->cv_submit.notify_all();
+  S->cv_done.notify_all();
+  return PUCK_OK;
+}
+
+int32_t puck_server_poll(puck_server* S, int64_t* ids, int32_t max_ids, int32_t wait_ms) {
+  if (!S || !ids || max_ids <= 0) return 0;
+  std::unique_lock<std::mutex> lk(S->mu);
+  if (S->done_q.empty() && wait_ms > 0)
+    S->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !S->done_q.empty(); });
+  int32_t k = 0;
+  while (k < max_ids && !S->done_q.empty()) {
+    ids[k++] = S->done_q.front();
+    S->done_q.pop_front();
+  }
+  return k;
+}
+
+puck_status puck_server_take(puck_server* S, int64_t id, puck_tree_node* nodes, int32_t max_nodes,
+                             int32_t* sent_status, int64_t* latency_ns) {
+  if (!S) return PUCK_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  auto it = S->reqs.find(id);
+  if (it == S->reqs.end() || it->second.t_done == 0) {
+    puck::set_last_error("puck_server_take: no finished request with this id");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  Request& r = it->second;
+  if (r.status == PUCK_OK && (!nodes || max_nodes < (int32_t)r.nodes.size())) {
+    puck::set_last_error("puck_server_take: node buffer smaller than 2n-1");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  if (r.status == PUCK_OK) std::memcpy(nodes, r.nodes.data(), r.nodes.size() * sizeof(puck_tree_node));
+  if (sent_status) *sent_status = r.status;
+  if (latency_ns) *latency_ns = r.t_done - r.t_arrival;
+  S->reqs.erase(it);
+  return PUCK_OK;
+}
+
+puck_status puck_server_get_stats(const puck_server* S, puck_server_stats* out) {
+  if (!S || !out) return PUCK_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  *out = S->stats;
+  return PUCK_OK;
+}
+
+}  // extern "C"
