@@ -163,9 +163,10 @@ def serving(path, levels, args, device: int):
     from puck_gb300.parser import pack_sentences
     from puck_gb300.server import CLServer, now_ns
     n = args.serve_sentences
-    sents = synth.lognormal_sentences(args.seed + 1000, n, 23, 1, 60, len(levels[1].words))
+    sents = synth.lognormal_sentences(args.seed + 1000, n, 23, 1, 60, len(levels[1].lex_offsets) - 1)
     words, offsets, lens = pack_sentences(sents)
-    S = CLServer(path, max_alloc_size=args.serve_mem_gb << 30, device=device, max_length=60, collect=False)
+    S = CLServer(path, max_alloc_size=args.serve_mem_gb << 30, device=device, max_length=60, collect=False,
+                 profile=True)
 
     def drain(count, want):
         lat, done_at = [], []
@@ -185,6 +186,7 @@ def serving(path, levels, args, device: int):
     for rate in args.serve_rates:
         gaps = rng.exponential(1.0 / rate, n)
         st0 = S.stats()
+        pm0 = [S.pass_ms(l) for l in range(len(levels))]
         t0 = now_ns() + 2_000_000
         sched = t0 + np.cumsum(gaps * 1e9).astype(np.int64)
         want = {}
@@ -228,7 +230,9 @@ def serving(path, levels, args, device: int):
                      "p99_ms": round(float(np.percentile(lat, 99)), 2),
                      "resident_peak": int(st1["resident_peak"]),
                      "ticks": int(st1["ticks"] - st0["ticks"]),
-                     "gpu_ms": round(st1["ms_device"] - st0["ms_device"], 1)})
+                     "gpu_ms": round(st1["ms_device"] - st0["ms_device"], 1),
+                     "pass_ms": {f"level{l}": [round(a - b, 1) for a, b in zip(S.pass_ms(l), pm0[l])]
+                                 for l in range(len(levels))}})
         log(f"serving {rate}/s: {rows[-1]}")
     S.close()
     return {"sentences_per_rate": n, "lengths": "lognormal mean 23 clipped 1-60",

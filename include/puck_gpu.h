@@ -199,6 +199,9 @@ int32_t puck_server_poll(puck_server* s, int64_t* ids, int32_t max_ids, int32_t 
 puck_status puck_server_take(puck_server* s, int64_t id, puck_tree_node* nodes, int32_t max_nodes,
                              int32_t* sent_status, int64_t* latency_ns);
 puck_status puck_server_get_stats(const puck_server* s, puck_server_stats* out);
+/* With opts.profile: CUDA-event ms of each step kind of one level summed over
+ * ticks, out[0..4] = lexicon, inside, outside, masks (+ scaling), decode. */
+puck_status puck_server_pass_ms(const puck_server* s, int32_t level, double out[5]);
 
 /* Last error message of the calling thread; returns the full length. */
 size_t puck_last_error(char* buf, size_t len);

@@ -55,7 +55,7 @@ EXPORTS = ("puck_default_options", "puck_grammar_load", "puck_grammar_free", "pu
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
            "puck_parser_stats", "puck_parser_pass_ms", "puck_mbr_decode_static", "puck_server_create",
            "puck_server_destroy", "puck_server_now_ns", "puck_server_submit", "puck_server_poll",
-           "puck_server_take", "puck_server_get_stats", "puck_last_error")
+           "puck_server_take", "puck_server_get_stats", "puck_server_pass_ms", "puck_last_error")
 
 _lib = None
 _lock = threading.Lock()
@@ -111,6 +111,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_server_take.restype = I
         L.puck_server_get_stats.argtypes = [P, ctypes.POINTER(ServerStats)]
         L.puck_server_get_stats.restype = I
+        L.puck_server_pass_ms.argtypes = [P, I, ctypes.POINTER(ctypes.c_double)]
+        L.puck_server_pass_ms.restype = I
         L.puck_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         L.puck_last_error.restype = ctypes.c_size_t
         _lib = L

@@ -76,41 +76,61 @@ __global__ void k_scaling(int cs, DevBatch B, DevWork W, const float* chart, flo
 }
 
 // ---------------------------------------------------------------------------
-// Viterbi backtrace: one warp per sentence.  Candidates are scanned in the
-// reference's sequential order (NT, TN, TT, NN by split) with ">=" ties, so
-// the winner is the last candidate that attains the maximum; lanes split the
-// rule lists and a (score, sequence index) reduction recovers that order.
+// Viterbi backtrace: one CTA per sentence, nodes in preorder.  Candidates are
+// numbered in the reference's sequential scan order (NT, TN, TT, then NN by
+// split) and compared with ">=", so the winner is the last candidate that
+// attains the maximum; the CTA's threads split the candidates and a (score,
+// sequence index) reduction recovers that order.
 struct Best { float score; int idx; int a, b, code; };
+
+__device__ __forceinline__ bool better(const Best& o, const Best& v) {
+  return o.score > v.score || (o.score == v.score && o.idx > v.idx);
+}
 
 __device__ __forceinline__ Best warp_argmax_last(Best v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    float os = __shfl_xor_sync(kFull, v.score, o);
-    int oi = __shfl_xor_sync(kFull, v.idx, o);
-    int oa = __shfl_xor_sync(kFull, v.a, o);
-    int ob = __shfl_xor_sync(kFull, v.b, o);
-    int oc = __shfl_xor_sync(kFull, v.code, o);
-    if (os > v.score || (os == v.score && oi > v.idx)) { v.score = os; v.idx = oi; v.a = oa; v.b = ob; v.code = oc; }
+    Best w;
+    w.score = __shfl_xor_sync(kFull, v.score, o);
+    w.idx = __shfl_xor_sync(kFull, v.idx, o);
+    w.a = __shfl_xor_sync(kFull, v.a, o);
+    w.b = __shfl_xor_sync(kFull, v.b, o);
+    w.code = __shfl_xor_sync(kFull, v.code, o);
+    if (better(w, v)) v = w;
   }
   return v;
 }
 
-__global__ void k_viterbi(DevLevel L, DevBatch B, DevWork W, int max_len, const float* inside, DevNode* nodes) {
-  extern __shared__ DevNode tn_all[];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const int k = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+constexpr int kVitThreads = 256;
+
+// CTA-wide argmax; every thread gets the result.
+__device__ __forceinline__ Best block_argmax_last(Best v, Best* red) {
+  v = warp_argmax_last(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();  // red is reused node after node
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  Best r = red[0];
+  for (int w = 1; w < kVitThreads / 32; ++w)
+    if (better(red[w], r)) r = red[w];
+  return r;
+}
+
+__global__ void __launch_bounds__(kVitThreads) k_viterbi(DevLevel L, DevBatch B, DevWork W, int max_len,
+                                                         const float* inside, DevNode* nodes) {
+  extern __shared__ DevNode tn[];
+  __shared__ Best red[kVitThreads / 32];
+  const int k = blockIdx.x;
   if (k >= W.nent) return;
   const int s = W.sent[k];
   const int n = B.len[s];
-  DevNode* tn = tn_all + wib * (2 * max_len - 1);
   const int cs = L.cell_size;
   const float* ibot = inside + B.cell_off[s] * cs;
   const float* itop = ibot + tri(n) * cs;
   auto CELL = [&](const float* base, int x, int y) { return base + (long long)cs * chart_index(x, y, n); };
   const int nnt = L.n_nt;
-  if (lane == 0) { tn[0].top = L.root; tn[0].width = n; tn[0].bot = 0; tn[0].score = 0.f; }
-  __syncwarp();
+  if (threadIdx.x == 0) { tn[0].top = L.root; tn[0].width = n; tn[0].bot = 0; tn[0].score = 0.f; }
+  __syncthreads();
   int begin = 0;
   for (int p = 0; p < 2 * n - 1; ++p) {
     const DevNode nd = tn[p];
@@ -121,37 +141,53 @@ __global__ void k_viterbi(DevLevel L, DevBatch B, DevWork W, int max_len, const 
       const float* child = CELL(ibot, begin, end);
       const int r0 = L.v_off[uoff], r1 = L.v_off[uoff + 1];
       Best bst{-30000.0f, -1, 0, 0, 0};
-      for (int r = r0 + lane; r < r1; r += 32) {
+      for (int r = r0 + threadIdx.x; r < r1; r += kVitThreads) {
         const int c = L.v_left[r];
         const float scr = L.v_score[r] + child[c];
         if (scr >= bst.score) { bst.score = scr; bst.idx = r; bst.a = c; }
       }
-      bst = warp_argmax_last(bst);
+      bst = block_argmax_last(bst, red);
       botSym = bst.idx < 0 ? 0 : bst.a;
-      if (lane == 0) { tn[p].bot = botSym; tn[p].score = bst.score; }
+      if (threadIdx.x == 0) { tn[p].bot = botSym; tn[p].score = bst.score; }
     }
     if (width == 1) {
-      if (lane == 0) tn[p].score = ibot[(long long)cs * begin + botSym];
+      if (threadIdx.x == 0) tn[p].score = ibot[(long long)cs * begin + botSym];
       begin += 1;
     } else {
+      // candidate t in [0, total): NT rules, TN rules, TT rules (width 2), then
+      // (width - 1) copies of the NN rules, one per split in ascending order
+      const int oNT = L.v_off[1 * nnt + botSym], nNT = L.v_off[1 * nnt + botSym + 1] - oNT;
+      const int oTN = L.v_off[2 * nnt + botSym], nTN = L.v_off[2 * nnt + botSym + 1] - oTN;
+      const int oTT = L.v_off[3 * nnt + botSym], nTT = width == 2 ? L.v_off[3 * nnt + botSym + 1] - oTT : 0;
+      const int oNN = L.v_off[botSym], nNN = L.v_off[botSym + 1] - oNN;
+      const int first = nNT + nTN + nTT;
+      const int total = first + (width - 1) * nNN;
+      const float* ntL = CELL(itop, begin, end - 1);
+      const float* ntR = CELL(ibot, end - 1, end);
+      const float* tnL = CELL(ibot, begin, begin + 1);
+      const float* tnR = CELL(itop, begin + 1, end);
+      const float* ttR = CELL(ibot, begin + 1, end);
       Best bst{-300000.0f, -1, 10, 10, begin + 1};
-      int base = 0;
-      auto scan = [&](const float* lc, const float* rc, int grp, int code) {
-        const int r0 = L.v_off[grp * nnt + botSym], r1 = L.v_off[grp * nnt + botSym + 1];
-        for (int r = r0 + lane; r < r1; r += 32) {
-          const int a = L.v_left[r], bb = L.v_right[r];
-          const float scr = (L.v_score[r] + lc[a]) + rc[bb];
-          if (scr >= bst.score) { bst.score = scr; bst.idx = base + (r - r0); bst.a = a; bst.b = bb; bst.code = code; }
+      for (int t = threadIdx.x; t < total; t += kVitThreads) {
+        int r, code;
+        const float *lc, *rc;
+        if (t < nNT) { r = oNT + t; lc = ntL; rc = ntR; code = -1; }
+        else if (t < nNT + nTN) { r = oTN + (t - nNT); lc = tnL; rc = tnR; code = -2; }
+        else if (t < first) { r = oTT + (t - nNT - nTN); lc = tnL; rc = ttR; code = -3; }
+        else {
+          const int q = t - first, j = q / nNN;
+          r = oNN + (q - j * nNN);
+          code = begin + 1 + j;
+          lc = CELL(itop, begin, code);
+          rc = CELL(itop, code, end);
         }
-        base += r1 - r0;
-      };
-      scan(CELL(itop, begin, end - 1), CELL(ibot, end - 1, end), 1, -1);
-      scan(CELL(ibot, begin, begin + 1), CELL(itop, begin + 1, end), 2, -2);
-      if (width == 2) scan(CELL(ibot, begin, begin + 1), CELL(ibot, begin + 1, end), 3, -3);
-      for (int sp = begin + 1; sp < end; ++sp) scan(CELL(itop, begin, sp), CELL(itop, sp, end), 0, sp);
-      bst = warp_argmax_last(bst);
+        const int a = L.v_left[r], bb = L.v_right[r];
+        const float scr = (L.v_score[r] + lc[a]) + rc[bb];
+        if (scr >= bst.score) { bst.score = scr; bst.idx = t; bst.a = a; bst.b = bb; bst.code = code; }
+      }
+      bst = block_argmax_last(bst, red);
       if (bst.idx < 0) { bst.a = 10; bst.b = 10; bst.code = begin + 1; }
-      if (lane == 0) {
+      if (threadIdx.x == 0) {
         tn[p].score = bst.score;
         int bestSplit = bst.code;
         const int cfg = bestSplit < 0 ? -bestSplit : 0;
@@ -164,10 +200,10 @@ __global__ void k_viterbi(DevLevel L, DevBatch B, DevWork W, int max_len, const 
         rn.width = end - bestSplit;
       }
     }
-    __syncwarp();
+    __syncthreads();
   }
   DevNode* out = nodes + B.node_off[s];
-  for (int p = lane; p < 2 * n - 1; p += 32) out[p] = tn[p];
+  for (int q = threadIdx.x; q < 2 * n - 1; q += kVitThreads) out[q] = tn[q];
 }
 
 // ---------------------------------------------------------------------------
@@ -260,12 +296,10 @@ cudaError_t launch_scaling(int cell_size, const DevBatch& B, const DevWork& W, c
 
 cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const DevWork& W, int max_len, const float* inside,
                            DevNode* nodes, cudaStream_t st) {
-  const int wpb = 4;
-  const int blocks = (W.nent + wpb - 1) / wpb;
-  if (blocks == 0) return cudaSuccess;
-  const size_t smem = (size_t)wpb * (2 * max_len - 1) * sizeof(DevNode);
+  if (W.nent == 0) return cudaSuccess;
+  const size_t smem = (size_t)(2 * max_len - 1) * sizeof(DevNode);
   set_smem(k_viterbi, smem);
-  k_viterbi<<<blocks, wpb * 32, smem, st>>>(L, B, W, max_len, inside, nodes);
+  k_viterbi<<<W.nent, kVitThreads, smem, st>>>(L, B, W, max_len, inside, nodes);
   return cudaGetLastError();
 }
 

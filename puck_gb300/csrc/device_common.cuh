@@ -30,6 +30,7 @@ __device__ __forceinline__ int entry_of(const DevWork& W, int i) {
 }
 
 __device__ __forceinline__ int span_of(const DevWork& W, int k) { return W.span ? W.span[k] : W.span_all; }
+__device__ __forceinline__ int ways_of(const DevWork& W, int k) { return W.ways ? W.ways[k] : W.ways_all; }
 
 // Semirings (src/main/scala/puck/parser/RuleSemiring.scala:22-98).
 template <int S> struct Sr;

@@ -50,6 +50,8 @@ struct CellCtx {
   unsigned words[kMaxMask];
   int nsp, nlive;
   int flag0, flag1;
+  int g, G;   // this CTA is part g of the cell's G parts
+  int last;
   unsigned long long work, corner;
 };
 
@@ -130,7 +132,7 @@ __device__ void gather_targets(const DevJob& J, const DevLevel& L, bool gated, f
     const int nc = min(chunk, nsp - c0);
     stage(X, c0, nc, cs, stA, stB);
     __syncthreads();
-    for (int t = warp; t < J.n_tgt; t += nwarps) {
+    for (int t = X.g * nwarps + warp; t < J.n_tgt; t += X.G * nwarps) {
       const int seg = __ldg(J.tgt_seg + t);
       if (seg < 0) continue;
       if (gated && !gate_hit(J, seg, ms, L.gate_merged, X.gate)) continue;
@@ -244,7 +246,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
     const int nlive = X.nlive;
-    for (int i = warp; i < nlive; i += nwarps) {
+    for (int i = X.g * nwarps + warp; i < nlive; i += X.G * nwarps) {
       const int p = sm.list[i];
       const int key = __ldg(J.pair_key + p);
       const int ca = key & 255, cb = (key >> 8) & 255;
@@ -377,6 +379,30 @@ __device__ __forceinline__ void store_cell(float* dst, const float* src, int cs)
     reinterpret_cast<float4*>(dst)[k] = reinterpret_cast<const float4*>(src)[k];
 }
 
+// Parts of a cell split over several CTAs: each part publishes its partial
+// row; the last part to arrive combines the rows in part order into P and
+// goes on to finish the cell.  Returns false for the parts that stop here.
+template <int S>
+__device__ bool combine_parts(const DevWork& W, CellCtx& X, float* P, int cs, long long cell) {
+  if (X.G == 1) return true;
+  store_cell(W.part_rows + (size_t)blockIdx.x * cs, P, cs);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) X.last = atomicAdd(W.cell_cnt + cell, 1) == X.G - 1;
+  __syncthreads();
+  if (!X.last) return false;
+  __threadfence();
+  const float* base = W.part_rows + (size_t)(blockIdx.x - X.g) * cs;
+  for (int k = threadIdx.x; k < cs; k += blockDim.x) {
+    float acc = Sr<S>::zero();
+    for (int j = 0; j < X.G; ++j) acc = Sr<S>::add(acc, j == X.g ? P[k] : __ldcg(base + (size_t)j * cs + k));
+    P[k] = acc;
+  }
+  if (threadIdx.x == 0) W.cell_cnt[cell] = 0;
+  __syncthreads();
+  return true;
+}
+
 __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
   if (threadIdx.x == 0) {
     if (X.work && C.work) atomicAdd(C.work, X.work);
@@ -398,7 +424,9 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
-  const int s = W.sent[ent], span = span_of(W, ent), b = (int)blockIdx.x - W.pref[ent], e = b + span, n = B.len[s];
+  const int s = W.sent[ent], span = span_of(W, ent), n = B.len[s];
+  const int G = ways_of(W, ent), local = (int)blockIdx.x - W.pref[ent];
+  const int b = local / G, e = b + span, g = local - (local / G) * G;
   const long long off = B.cell_off[s], toff = off + tri(n);
   const long long pbot = off + chart_index(b, e, n), ptop = toff + chart_index(b, e, n);
   if (threadIdx.x == 0) {
@@ -406,11 +434,15 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
     X.flag1 = mask_any(M, ptop);
     X.work = 0;
     X.corner = 0;
+    // a pruned cell has no rule work: part 0 finishes it alone
+    X.G = X.flag0 && span >= 2 ? G : 1;
+    X.g = X.flag0 && span >= 2 ? g : 0;
     if (M.bits)
       for (int i = 0; i < ms; ++i) X.gate[i] = M.bits[pbot * ms + i];
   }
   for (int k = threadIdx.x; k < cs; k += blockDim.x) P[k] = Sr<S>::zero();
   __syncthreads();
+  if (X.G == 1 && g != 0) return;  // a spare part of a pruned cell
   const bool gated = M.bits != nullptr;
   const float ps = S == SEMI_REAL ? scale_of(M.iscale, pbot) : 0.f;
   auto BOT = [&](int x, int y) { return off + chart_index(x, y, n); };
@@ -440,6 +472,10 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
     }
   }
   __syncthreads();
+  if (!combine_parts<S>(W, X, P, cs, pbot)) {
+    flush_counters(X, C);
+    return;
+  }
   if (span >= 2) {
     store_cell(inside + pbot * cs, P, cs);
     live_bits<S>(P, L.n_nt, L.nt_coarse, ms, X, V.in + pbot * ms);
@@ -468,7 +504,9 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
-  const int s = W.sent[ent], span = span_of(W, ent), b = (int)blockIdx.x - W.pref[ent], e = b + span, n = B.len[s];
+  const int s = W.sent[ent], span = span_of(W, ent), n = B.len[s];
+  const int G = ways_of(W, ent), local = (int)blockIdx.x - W.pref[ent];
+  const int b = local / G, e = b + span, g = local - (local / G) * G;
   const long long off = B.cell_off[s], toff = off + tri(n);
   const long long cbot = off + chart_index(b, e, n), ctop = toff + chart_index(b, e, n);
   auto BOT = [&](int x, int y) { return off + chart_index(x, y, n); };
@@ -479,11 +517,17 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
     X.flag1 = mask_any(M, cbot);
     X.work = 0;
     X.corner = 0;
+    // parts split the parent gathers of span >= 2 (span 1 runs a second
+    // gather after its unary layer and is never split)
+    const bool parts = X.flag0 && span >= 2 && span != n;
+    X.G = parts ? G : 1;
+    X.g = parts ? g : 0;
     if (M.bits)
       for (int i = 0; i < ms; ++i) X.gate[i] = M.bits[ctop * ms + i];
   }
   for (int k = threadIdx.x; k < cs; k += blockDim.x) P[k] = Sr<S>::zero();
   __syncthreads();
+  if (X.G == 1 && g != 0) return;  // a spare part of a cell without parent gathers
   const float* IS = M.iscale;
   const float* OS = M.oscale;
   // operand helpers: (outside parent, inside sibling) or (inside sibling, outside parent)
@@ -522,6 +566,10 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
     }
   }
   __syncthreads();
+  if (!combine_parts<S>(W, X, P, cs, ctop)) {
+    flush_counters(X, C);
+    return;
+  }
   store_cell(outside + ctop * cs, P, cs);
   live_bits<S>(P, L.n_nt, L.nt_coarse, ms, X, V.out ? V.out + ctop * ms : nullptr);
   // unary layer: outside-bot from outside-top.  With a batch of one-word

@@ -91,6 +91,11 @@ struct DevBatch {
 // k with pref[k] <= i < pref[k+1].  Units are cells of one span length per
 // entry (span passes), tokens (lexicon), cells (per-cell kernels) or whole
 // sentences (decoders).  One launch can mix sentences at different spans.
+// A span pass may give each cell of an entry `ways` CTAs: unit
+// pref[k] + c * ways + g is part g of cell c.  The parts split the cell's rule
+// work, leave partial rows in part_rows (one row per unit), and the last part
+// to finish (counted in cell_cnt, indexed by chart cell, zero between
+// launches) combines them and finishes the cell.
 struct DevWork {
   int nent;
   long long nunits;         // pref[nent], kept on the host side for grid sizes
@@ -98,6 +103,10 @@ struct DevWork {
   const int* span;          // [nent] span length of the entry's cells; null: span_all for every entry
   int span_all;
   const int* pref;          // [nent + 1]; null for per-sentence launches (unit k is entry k)
+  const int* ways;          // [nent] CTAs per cell; null: ways_all
+  int ways_all;
+  float* part_rows;         // [nunits * cell_size] when any entry has ways > 1
+  int* cell_cnt;            // [cells of the chart]
   int one_word_batch;       // outside pass: the reference's batch-of-one-word-sentences unary quirk
 };
 
@@ -150,6 +159,22 @@ cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWo
                                const float* inside, const double* part_scale, float* log_z, cudaStream_t st);
 
 size_t pass_smem_bytes(const DevLevel& L, int chunk);
+
+// CTAs per cell of a span launch.  A cell's rule work grows with its split
+// count (span - 1).  part_target(total, sms) is the work one part should get:
+// the launch's total split count spread over two waves of CTAs (five per SM),
+// and at least four splits; cell_ways gives a cell enough parts for that, at
+// most 16.  A launch that already fills the GPU keeps one CTA per cell.
+inline double part_target(double total_splits, int sms) {
+  const double t = total_splits / (2.0 * sms * 5);
+  return t < 4.0 ? 4.0 : t;
+}
+inline int cell_ways(int span, double target) {
+  if (span < 4) return 1;
+  int g = (int)((span - 1 + target - 1e-9) / target);
+  if (g > 16) g = 16;
+  return g < 1 ? 1 : g;
+}
 
 // Message returned by puck_last_error on the calling thread.
 void set_last_error(const char* msg);

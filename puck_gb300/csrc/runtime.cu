@@ -411,7 +411,8 @@ struct puck_parser {
   std::vector<std::unique_ptr<LevelDev>> levels;
   std::vector<LevelBufs> bufs;
   DevBuf b_len, b_cell_off, b_word_off, b_words, b_work, b_node_off,
-      b_mbr_off, b_nodes, b_status, b_logz, b_scratch, b_counters;
+      b_mbr_off, b_nodes, b_status, b_logz, b_scratch, b_counters, b_parts, b_cell_cnt;
+  int sms = 1;
   puck::DevBatch last_batch{};
   int64_t last_num_cells = 0;
   int last_batches = 0;
@@ -487,10 +488,16 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     return at;
   };
   std::vector<ListAt> span_list(max_len + 1);
+  std::vector<int> ways(max_len + 1, 1);
+  long long part_units = 0;
   for (int L = 1; L <= max_len; ++L) {
     int k = 0;
-    while (k < ns && len[order[k]] >= L) ++k;
-    span_list[L] = add_list(k, [&](int j) { return order[j]; }, [&](int j) { return len[order[j]] - L + 1; });
+    long long cells = 0;
+    while (k < ns && len[order[k]] >= L) cells += len[order[k++]] - L + 1;
+    const int G = puck::cell_ways(L, puck::part_target((double)cells * (L - 1), P->sms));
+    ways[L] = G;
+    if (G > 1) part_units = std::max(part_units, cells * G);
+    span_list[L] = add_list(k, [&](int j) { return order[j]; }, [&](int j) { return (len[order[j]] - L + 1) * G; });
   }
   const ListAt tok_list = add_list(ns, [](int j) { return j; }, [&](int j) { return len[j]; });
   const ListAt cell_list = add_list(ns, [](int j) { return j; }, [&](int j) { return 2 * tri(len[j]); });
@@ -522,6 +529,10 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     W.span = nullptr;
     W.span_all = span;
     W.pref = wdev + a.pref;
+    W.ways = nullptr;
+    W.ways_all = span >= 1 && span <= max_len ? ways[span] : 1;
+    W.part_rows = P->b_parts.as<float>();
+    W.cell_cnt = P->b_cell_cnt.as<int>();
     W.one_word_batch = max_len == 1;
     return W;
   };
@@ -533,6 +544,13 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   CUDA_TRY(cudaMemsetAsync(P->b_status.p, 0, ns * sizeof(int), st));
   P->b_counters.ensure(64);
   CUDA_TRY(cudaMemsetAsync(P->b_counters.p, 0, 64, st));
+  if (part_units > 0) {
+    int max_cs = 0;
+    for (const HostLevel& HL : P->g->levels) max_cs = std::max(max_cs, HL.cell_size);
+    P->b_parts.ensure(part_units * max_cs * sizeof(float));
+  }
+  P->b_cell_cnt.ensure(num_cells * sizeof(int) + 16);
+  CUDA_TRY(cudaMemsetAsync(P->b_cell_cnt.p, 0, num_cells * sizeof(int), st));
   puck::Counters C{P->b_counters.as<unsigned long long>(), P->b_counters.as<unsigned long long>() + 1,
                    P->b_status.as<int>()};
 
@@ -834,6 +852,7 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
     CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (P->opt.device < 0 || P->opt.device >= ndev) throw PuckError{PUCK_ERR_INVALID_ARG, "no such CUDA device"};
     CUDA_TRY(cudaSetDevice(P->opt.device));
+    CUDA_TRY(cudaDeviceGetAttribute(&P->sms, cudaDevAttrMultiProcessorCount, P->opt.device));
     CUDA_TRY(cudaStreamCreateWithFlags(&P->stream, cudaStreamNonBlocking));
     const int nl = (int)g->levels.size();
     for (auto& e : P->ev_batch) CUDA_TRY(cudaEventCreate(&e));
@@ -869,7 +888,7 @@ void puck_parser_destroy(puck_parser* P) {
     b.part.release(); b.decode.release(); b.live_in.release(); b.live_out.release();
   }
   for (DevBuf* b : {&P->b_len, &P->b_cell_off, &P->b_word_off, &P->b_words, &P->b_work, &P->b_node_off, &P->b_mbr_off, &P->b_nodes, &P->b_status,
-                    &P->b_logz, &P->b_scratch, &P->b_counters})
+                    &P->b_logz, &P->b_scratch, &P->b_counters, &P->b_parts, &P->b_cell_cnt})
     b->release();
   P->levels.clear();
   for (auto& e : P->ev_batch)

@@ -31,6 +31,7 @@
 
 #include "host_runtime.h"
 
+#include <array>
 #include <chrono>
 #include <climits>
 #include <condition_variable>
@@ -166,6 +167,7 @@ struct TickBuf {
   puck::DevNode* out_dev = nullptr;
   size_t out_cap = 0;  // nodes
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  std::vector<cudaEvent_t> ev_group;  // profile: after the slot update, then after each step group
   std::vector<Finishing> finishing;
   int64_t launches = 0, h2d = 0, d2h = 0;
 };
@@ -177,13 +179,14 @@ struct LevelArena {
 
 // One step list of a tick: entries (slot, span) and the unit prefix.
 struct StepList {
-  std::vector<int> sent, span, pref;
+  std::vector<int> sent, span, pref, ways;
   long long units = 0;
-  size_t at_sent = 0, at_span = 0, at_pref = 0;  // byte offsets in the staging buffer
+  size_t at_sent = 0, at_span = 0, at_pref = 0, at_ways = 0;  // byte offsets in the staging buffer
   void clear() {
     sent.clear();
     span.clear();
     pref.clear();
+    ways.clear();
     units = 0;
   }
 };
@@ -198,8 +201,9 @@ struct puck_server {
   cudaStream_t stream = nullptr;
   std::vector<std::unique_ptr<LevelDev>> levels;
   std::vector<LevelArena> la;
-  DevBuf d_len, d_cell_off, d_node_off, d_mbr_off, d_words, d_status, d_counters, d_decode, d_scratch;
-  int slots = 0;
+  DevBuf d_len, d_cell_off, d_node_off, d_mbr_off, d_words, d_status, d_counters, d_decode, d_scratch, d_parts,
+      d_cell_cnt;
+  int slots = 0, sms = 1, max_cs = 0;
   CellArena arena;
   std::vector<int> free_slots;
   TickBuf tb[2];
@@ -214,6 +218,7 @@ struct puck_server {
   int64_t next_id = 0;
   bool stopping = false;
   puck_server_stats stats{};
+  std::vector<std::array<double, 5>> pass_ms;  // per level: lexicon, inside, outside, masks, decode
   std::thread loop;
 };
 
@@ -308,8 +313,14 @@ void harvest(puck_server* S, int p) {
   CUDA_TRY(cudaEventSynchronize(T.ev_end));
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, T.ev_begin, T.ev_end));
+  std::vector<float> gms(T.ev_group.size() > 1 ? T.ev_group.size() - 1 : 0, 0.f);
+  for (size_t k = 0; k < gms.size(); ++k) CUDA_TRY(cudaEventElapsedTime(&gms[k], T.ev_group[k], T.ev_group[k + 1]));
   const int64_t t = now_ns();
   std::lock_guard<std::mutex> lk(S->mu);
+  for (size_t k = 0; k < gms.size(); ++k) {
+    const int level = std::min<int>((int)k / 4, S->nl - 1), kind = (int)k < 4 * S->nl ? (int)k % 4 : 4;
+    S->pass_ms[level][kind] += gms[k];
+  }
   for (const Finishing& f : T.finishing) {
     Request& r = S->reqs[f.id];
     r.nodes.assign(T.out_host + f.node_at, T.out_host + f.node_at + (2 * f.n - 1));
@@ -411,6 +422,26 @@ bool run_tick(puck_server* S, int p) {
     L.span.swap(p2);
     L.pref.swap(u2);
   }
+  // span lists: CTAs per cell from the launch's total cell count
+  long long part_units = 0;
+  for (auto& L : lists) {
+    if (L.span.empty()) continue;
+    double splits = 0;
+    for (size_t k = 0; k < L.sent.size(); ++k) splits += (double)L.pref[k] * std::max(L.span[k] - 1, 1);
+    const double target = puck::part_target(splits, S->sms);
+    L.ways.resize(L.sent.size());
+    bool split = false;
+    for (size_t k = 0; k < L.sent.size(); ++k) {
+      L.ways[k] = puck::cell_ways(L.span[k], target);
+      L.pref[k] *= L.ways[k];
+      split |= L.ways[k] > 1;
+    }
+    if (split) {
+      long long u = 0;
+      for (int x : L.pref) u += x;
+      part_units = std::max(part_units, u);
+    }
+  }
   for (auto& L : lists) {
     long long acc = 0;
     std::vector<int> pref(L.pref.size() + 1, 0);
@@ -436,6 +467,7 @@ bool run_tick(puck_server* S, int p) {
     L.at_sent = section(L.sent.size() * sizeof(int));
     L.at_span = section(L.span.size() * sizeof(int));
     L.at_pref = section(L.pref.size() * sizeof(int));
+    L.at_ways = section(L.ways.size() * sizeof(int));
   }
   ensure_host(T.host, T.host_cap, bytes);
   std::memcpy(T.host + at_upd, upd.data(), upd.size() * sizeof(SlotUpdate));
@@ -444,7 +476,9 @@ bool run_tick(puck_server* S, int p) {
     std::memcpy(T.host + L.at_sent, L.sent.data(), L.sent.size() * sizeof(int));
     std::memcpy(T.host + L.at_span, L.span.data(), L.span.size() * sizeof(int));
     std::memcpy(T.host + L.at_pref, L.pref.data(), L.pref.size() * sizeof(int));
+    std::memcpy(T.host + L.at_ways, L.ways.data(), L.ways.size() * sizeof(int));
   }
+  if (part_units > 0) S->d_parts.ensure(part_units * S->max_cs * sizeof(float));
   T.dev.ensure(std::max<size_t>(bytes, 16));
   ensure_out(T, (size_t)out_nodes);
   cudaStream_t st = S->stream;
@@ -492,10 +526,19 @@ bool run_tick(puck_server* S, int p) {
     W.span = L.span.empty() ? nullptr : reinterpret_cast<const int*>(dbase + L.at_span);
     W.span_all = 0;
     W.pref = reinterpret_cast<const int*>(dbase + L.at_pref);
+    W.ways = L.ways.empty() ? nullptr : reinterpret_cast<const int*>(dbase + L.at_ways);
+    W.ways_all = 1;
+    W.part_rows = S->d_parts.as<float>();
+    W.cell_cnt = S->d_cell_cnt.as<int>();
     W.one_word_batch = 0;
     return W;
   };
   const int maxlen = S->opt.max_length;
+  const bool prof = !T.ev_group.empty();
+  auto mark = [&](int k) {
+    if (prof) CUDA_TRY(cudaEventRecord(T.ev_group[k], st));
+  };
+  mark(0);
   puck::DevMask M{nullptr, 0, nullptr, nullptr};
   for (int l = 0; l < S->nl; ++l) {
     const puck::DevLevel& D = S->levels[l]->d;
@@ -513,14 +556,17 @@ bool run_tick(puck_server* S, int p) {
       CUDA_TRY(puck::launch_lexicon(D, B, work(Llex), MM, inside, A.part.as<double>(), V, C, st));
       ++T.launches;
     }
+    mark(4 * l + 1);
     if (!Lin.sent.empty()) {
       CUDA_TRY(puck::launch_inside_span(D, B, work(Lin), MM, maxlen, inside, V, C, st));
       ++T.launches;
     }
+    mark(4 * l + 2);
     if (!Lout.sent.empty()) {
       CUDA_TRY(puck::launch_outside_span(D, B, work(Lout), MM, maxlen, inside, outside, V, C, st));
       ++T.launches;
     }
+    mark(4 * l + 3);
     if (!A.last) {
       if (!Lmask.sent.empty()) {
         const puck::DevWork W = work(Lmask);
@@ -536,10 +582,15 @@ bool run_tick(puck_server* S, int p) {
       M.mask_size = D.mask_size;
       M.iscale = A.next_real ? A.iscale.as<float>() : nullptr;
       M.oscale = A.next_real ? A.oscale.as<float>() : nullptr;
+      mark(4 * l + 4);
       continue;
     }
+    mark(4 * l + 4);
     const StepList& Ldec = lists[4 * S->nl];
-    if (Ldec.sent.empty()) continue;
+    if (Ldec.sent.empty()) {
+      mark(4 * S->nl + 1);
+      continue;
+    }
     puck::DevWork W = work(Ldec);
     if (!S->mbr) {
       CUDA_TRY(puck::launch_viterbi(D, B, W, maxlen, inside, T.out_dev, st));
@@ -551,6 +602,7 @@ bool run_tick(puck_server* S, int p) {
                                        S->d_mbr_off.as<long long>(), S->d_scratch.as<float>(), T.out_dev, st));
       T.launches += 2;
     }
+    mark(4 * S->nl + 1);
   }
   CUDA_TRY(cudaEventRecord(T.ev_end, st));
   {
@@ -600,7 +652,7 @@ void loop_main(puck_server* S) {
 }
 
 int64_t server_bytes_per_cell(const puck_server* S) {
-  int64_t b = 4;  // the sentence's words at its first cells
+  int64_t b = 8;  // the sentence's words at its first cells; the cell's part counter
   for (int l = 0; l < S->nl; ++l) {
     const HostLevel& L = S->g->levels[l];
     const LevelArena& A = S->la[l];
@@ -621,12 +673,13 @@ void destroy_server(puck_server* S) {
     T.dev.release();
     if (T.ev_begin) cudaEventDestroy(T.ev_begin);
     if (T.ev_end) cudaEventDestroy(T.ev_end);
+    for (cudaEvent_t e : T.ev_group) cudaEventDestroy(e);
   }
   for (LevelArena& A : S->la)
     for (DevBuf* b : {&A.inside, &A.outside, &A.live_in, &A.live_out, &A.masks, &A.iscale, &A.oscale, &A.part})
       b->release();
   for (DevBuf* b : {&S->d_len, &S->d_cell_off, &S->d_node_off, &S->d_mbr_off, &S->d_words, &S->d_status,
-                    &S->d_counters, &S->d_decode, &S->d_scratch})
+                    &S->d_counters, &S->d_decode, &S->d_scratch, &S->d_parts, &S->d_cell_cnt})
     b->release();
   S->levels.clear();
   if (S->stream) cudaStreamDestroy(S->stream);
@@ -664,10 +717,18 @@ puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts,
     CUDA_TRY(cudaGetDeviceCount(&ndev));
     if (S->opt.device < 0 || S->opt.device >= ndev) throw PuckError{PUCK_ERR_INVALID_ARG, "no such CUDA device"};
     CUDA_TRY(cudaSetDevice(S->opt.device));
+    CUDA_TRY(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->opt.device));
     CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
     for (TickBuf& T : S->tb) {
       CUDA_TRY(cudaEventCreate(&T.ev_begin));
       CUDA_TRY(cudaEventCreate(&T.ev_end));
+    }
+    S->nl = (int)g->levels.size();
+    S->pass_ms.assign(S->nl, std::array<double, 5>{0, 0, 0, 0, 0});
+    for (TickBuf& T : S->tb) {
+      if (!S->opt.profile) continue;
+      T.ev_group.resize(4 * S->nl + 2);
+      for (cudaEvent_t& e : T.ev_group) CUDA_TRY(cudaEventCreate(&e));
     }
     for (int l = 0; l < S->nl; ++l) {
       S->levels.emplace_back(new LevelDev());
@@ -715,6 +776,9 @@ puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts,
     S->d_words.ensure(cells * sizeof(int));
     S->d_counters.ensure(64);
     CUDA_TRY(cudaMemsetAsync(S->d_counters.p, 0, 64, S->stream));
+    S->d_cell_cnt.ensure(cells * sizeof(int));
+    CUDA_TRY(cudaMemsetAsync(S->d_cell_cnt.p, 0, cells * sizeof(int), S->stream));
+    for (const HostLevel& HL : g->levels) S->max_cs = std::max(S->max_cs, HL.cell_size);
     if (S->mbr) {
       S->d_decode.ensure(cells * sizeof(float2));
       S->d_scratch.ensure(6 * cells * sizeof(float));
@@ -830,6 +894,13 @@ puck_status puck_server_get_stats(const puck_server* S, puck_server_stats* out) 
   if (!S || !out) return PUCK_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> lk(S->mu);
   *out = S->stats;
+  return PUCK_OK;
+}
+
+puck_status puck_server_pass_ms(const puck_server* S, int32_t level, double out[5]) {
+  if (!S || !out || level < 0 || level >= S->nl) return PUCK_ERR_INVALID_ARG;
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (int k = 0; k < 5; ++k) out[k] = S->pass_ms[level][k];
   return PUCK_OK;
 }
 

@@ -34,7 +34,7 @@ class CLServer:
 
     def __init__(self, grammar_path: str, max_alloc_size: int = 1 << 30, device: int = 0,
                  decode: str = "auto", max_length: int = 100, prune_threshold: float = -9.0,
-                 max_resident: int = 0, collect: bool = True):
+                 max_resident: int = 0, collect: bool = True, profile: bool = False):
         """collect=True starts a thread that takes finished requests and
         completes their futures; with collect=False the caller drives
         ``poll``/``take`` itself."""
@@ -53,6 +53,7 @@ class CLServer:
         opt.max_length = max_length
         opt.prune_threshold = prune_threshold
         opt.max_batch_sentences = max_resident
+        opt.profile = 1 if profile else 0
         self._s = L.puck_server_create(self._g, ctypes.byref(opt), ctypes.byref(st))
         if not self._s:
             err = _lib.last_error()
@@ -97,6 +98,13 @@ class CLServer:
         s = _lib.ServerStats()
         _lib.check(self._L.puck_server_get_stats(self._s, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in s._fields_}
+
+    def pass_ms(self, level: int) -> List[float]:
+        """[lexicon, inside, outside, masks, decode] CUDA-event ms of one level
+        summed over ticks (needs profile=True)."""
+        out = (ctypes.c_double * 5)()
+        _lib.check(self._L.puck_server_pass_ms(self._s, level, out))
+        return list(out)
 
     # -- future-based API -------------------------------------------------------
     def _word_ids(self, sentence: Sequence[Union[str, int]]) -> List[int]:
