@@ -45,6 +45,7 @@ sys.path.insert(0, ROOT)
 
 N_SENT = 20000
 MAX_LEN = 40
+FINE_INSIDE_BYTES_PER_UNIT = 0.08112
 
 
 def log(*a):
@@ -289,7 +290,7 @@ def run_ours(args):
             ev[k][1].record()
             s = P.stats()
             dev_ms.append(s["ms_device"])
-            work += s["binary_work"]
+            work += P.level_work(len(levels) - 1)[0]
             launches += s["kernel_launches"]
             h2d, d2h = s["h2d_bytes"], s["d2h_bytes"]
             ms, n = P.pass_ms(len(levels) - 1)
@@ -313,6 +314,11 @@ def run_ours(args):
     per_launch_ops = 2.0 * work / max(fine_in_launch, 1)
     avg_launch_s = fine_in_ms / 1e3 / max(fine_in_launch, 1)
     achieved = per_launch_ops / avg_launch_s / 1e12
+    # DRAM traffic per work unit of the fine inside kernel, measured with ncu
+    # over all fine inside launches of a 2,000-sentence run of this workload
+    # (profiles/traffic_k_inside_span_split_viterbi_2000.md), scaled to this
+    # run's average launch
+    traffic = FINE_INSIDE_BYTES_PER_UNIT * work / max(fine_in_launch, 1)
     out = {
         "metric": "sentences/sec, 1.1k-symbol grammar, len<=40 (batched/served vs plain); p50/p99 ms",
         "value": round(value, 2), "unit": "sentences/s", "n_gpus": world, "steps": args.steps,
@@ -332,7 +338,9 @@ def run_ours(args):
         "clocks": clocks,
         "roofline": {"bound": "alu", "kernel": "k_inside_span<viterbi> (fine level)",
                      "achieved": round(achieved, 3), "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
-                     "frac": round(achieved / fp32_peak, 4), "traffic": None,
+                     "frac": round(achieved / fp32_peak, 4), "traffic": round(traffic),
+                     "traffic_unit": "bytes per launch (ncu, scaled by work units)",
+                     "traffic_gbs": round(traffic / avg_launch_s / 1e9, 1),
                      "note": "FP32 max-plus on CUDA cores: ops = 2 x (sum over cells of live splits x child "
                              "pairs + applied rules); peak = 152 SMs x 128 FP32 lanes x measured max SM clock",
                      "work_per_launch": round(work / max(fine_in_launch, 1)),

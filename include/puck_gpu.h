@@ -132,6 +132,11 @@ puck_status puck_parser_stats(const puck_parser* p, puck_stats* out);
  * out[0] inside, out[1] outside, out[2] masks + scaling, out[3] decode (ms);
  * launches[0..3] the matching kernel launch counts. */
 puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[4], int64_t launches[4]);
+/* Binary-rule work of one level in the last call: out[0] = work units (the
+ * pair-factored form: live split x child-pair elements plus applied rules;
+ * the target-major form: rule x split applications), out[1] = binary partials
+ * >= +0.0 (Viterbi), which the reference's atomic_min would have dropped. */
+puck_status puck_parser_level_work(const puck_parser* p, int32_t level, int64_t out[2]);
 
 /* Max-constituent (MBR) tree decode into caller-owned device buffers with no
  * device allocation, for callers that cannot allocate at the point where they

@@ -422,6 +422,7 @@ struct puck_parser {
   std::vector<std::array<cudaEvent_t, 5>> ev_level;   // per level: in0, in1, out1, mask1, dec1
   std::vector<std::array<double, 4>> pass_ms;
   std::vector<std::array<int64_t, 4>> pass_launches;
+  std::vector<std::array<int64_t, 2>> level_work;  // per level: work units, +0.0 partials (last call)
 };
 
 namespace {
@@ -542,8 +543,10 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   Wsent.nunits = ns;
   P->b_status.ensure(ns * sizeof(int) + 16);
   CUDA_TRY(cudaMemsetAsync(P->b_status.p, 0, ns * sizeof(int), st));
-  P->b_counters.ensure(64);
-  CUDA_TRY(cudaMemsetAsync(P->b_counters.p, 0, 64, st));
+  // per level: binary partials >= +0.0 written, (rule, split) work units
+  const size_t ctr_bytes = 2 * nl * sizeof(unsigned long long);
+  P->b_counters.ensure(ctr_bytes);
+  CUDA_TRY(cudaMemsetAsync(P->b_counters.p, 0, ctr_bytes, st));
   if (part_units > 0) {
     int max_cs = 0;
     for (const HostLevel& HL : P->g->levels) max_cs = std::max(max_cs, HL.cell_size);
@@ -551,8 +554,6 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   }
   P->b_cell_cnt.ensure(num_cells * sizeof(int) + 16);
   CUDA_TRY(cudaMemsetAsync(P->b_cell_cnt.p, 0, num_cells * sizeof(int), st));
-  puck::Counters C{P->b_counters.as<unsigned long long>(), P->b_counters.as<unsigned long long>() + 1,
-                   P->b_status.as<int>()};
 
   auto rec = [&](cudaEvent_t e) { CUDA_TRY(cudaEventRecord(e, st)); };
   std::vector<std::array<int64_t, 4>> launches_l(nl, std::array<int64_t, 4>{0, 0, 0, 0});
@@ -579,6 +580,8 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     auto& EV = P->ev_level[l];
     auto& LC = launches_l[l];
     rec(EV[0]);
+    const puck::Counters C{P->b_counters.as<unsigned long long>() + 2 * l,
+                           P->b_counters.as<unsigned long long>() + 2 * l + 1, P->b_status.as<int>()};
     CUDA_TRY(puck::launch_lexicon(D, B, Wtok, MM, inside, lb.part.as<double>(), V, C, st));
     ++LC[0];
     for (int span = 1; span <= max_len; ++span) {
@@ -678,9 +681,9 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     }
   }
   std::vector<int> status(ns);
-  unsigned long long ctr[2] = {0, 0};
+  std::vector<unsigned long long> ctr(2 * nl, 0);
   CUDA_TRY(cudaMemcpyAsync(status.data(), P->b_status.p, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaMemcpyAsync(ctr, P->b_counters.p, sizeof(ctr), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaMemcpyAsync(ctr.data(), P->b_counters.p, ctr_bytes, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
   if (sent_status)
     for (int i = 0; i < ns; ++i)
@@ -707,7 +710,11 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   }
   P->stats.ms_device += ms_between(P->ev_batch[0], P->ev_batch[1]);
   P->stats.cells += num_cells;
-  P->stats.binary_work += (int64_t)ctr[1];
+  for (int l = 0; l < nl; ++l) {
+    P->stats.binary_work += (int64_t)ctr[2 * l + 1];
+    P->level_work[l][0] += (int64_t)ctr[2 * l + 1];
+    P->level_work[l][1] += (int64_t)ctr[2 * l];
+  }
   P->stats.kernel_launches += launches;
   P->stats.batches += 1;
   P->last_batch = B;
@@ -724,6 +731,7 @@ puck_status run_call(puck_parser* P, Mode mode, const int32_t* word_ids, const i
     P->stats = puck_stats{};
     for (auto& a : P->pass_ms) a = {0, 0, 0, 0};
     for (auto& a : P->pass_launches) a = {0, 0, 0, 0};
+    for (auto& a : P->level_work) a = {0, 0};
     const int nwords = P->g->levels.back().n_words;
     std::vector<int64_t> node_off(nsent + 1, 0);
     std::vector<int> valid;
@@ -861,6 +869,7 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
       for (auto& e : a) CUDA_TRY(cudaEventCreate(&e));
     P->pass_ms.assign(nl, std::array<double, 4>{0, 0, 0, 0});
     P->pass_launches.assign(nl, std::array<int64_t, 4>{0, 0, 0, 0});
+    P->level_work.assign(nl, std::array<int64_t, 2>{0, 0});
     for (int l = 0; l < nl; ++l) {
       P->levels.emplace_back(new LevelDev());
       build_level(*P->levels.back(), g->levels[l], l < nl - 1 && nl != 1);
@@ -958,6 +967,16 @@ puck_status puck_debug_copy(puck_parser* P, int32_t level, int32_t which, void* 
 puck_status puck_parser_stats(const puck_parser* p, puck_stats* out) {
   if (!p || !out) return PUCK_ERR_INVALID_ARG;
   *out = p->stats;
+  return PUCK_OK;
+}
+
+puck_status puck_parser_level_work(const puck_parser* p, int32_t level, int64_t out[2]) {
+  if (!p || !out || level < 0 || level >= (int)p->level_work.size()) {
+    set_error("bad level");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  out[0] = p->level_work[level][0];
+  out[1] = p->level_work[level][1];
   return PUCK_OK;
 }
 

@@ -314,6 +314,12 @@ class CLParser:
         _lib.check(self._L.puck_parser_pass_ms(self._p, level, ms, n))
         return list(ms), list(n)
 
+    def level_work(self, level: int):
+        """(binary work units, +0.0 partials) of one level in the last call."""
+        out = (ctypes.c_int64 * 2)()
+        _lib.check(self._L.puck_parser_level_work(self._p, level, out))
+        return int(out[0]), int(out[1])
+
     def release(self) -> None:
         if getattr(self, "_p", None):
             self._L.puck_parser_destroy(self._p)
