@@ -52,16 +52,33 @@ def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
 
-def workload(seed: int, n_sent: int, grammar_seed: int = 1):
+def workload(seed: int, n_sent: int, grammar_seed: int = 1, fine_semiring: str = "viterbi"):
     import numpy as np
     from puck_gb300 import grammar, grz, synth
     t0 = time.time()
     c, f = synth.split_grammar(seed=grammar_seed)
-    levels = [grammar.compile_level(c, "viterbi"), grammar.compile_level(f, "viterbi")]
-    path = os.path.join(tempfile.gettempdir(), f"puck_bench_split_{grammar_seed}_{os.getpid()}.grz")
+    levels = [grammar.compile_level(c, "viterbi"), grammar.compile_level(f, fine_semiring)]
+    path = os.path.join(tempfile.gettempdir(),
+                        f"puck_bench_split_{grammar_seed}_{fine_semiring}_{os.getpid()}.grz")
     grz.write_sequence(path, levels)
     sents = synth.lognormal_sentences(seed, n_sent, 23, 1, MAX_LEN, len(f.words))
     log(f"workload ready in {time.time() - t0:.1f}s: fine nt={levels[1].n_nt} t={levels[1].n_t} "
+        f"rules={f.bin_rules.shape[0]} sentences={n_sent} mean_len={np.mean([len(s) for s in sents]):.2f}")
+    return levels, path, sents
+
+
+def long_workload(seed: int, n_sent: int):
+    """Long-sentence stress grammar: ~2,000 fine symbols (splits up to 32),
+    ~4M binaries; lengths uniform in 41-100."""
+    import numpy as np
+    from puck_gb300 import grammar, grz, synth
+    t0 = time.time()
+    c, f = synth.split_grammar(seed=5, max_split=32, mean_split=20.4, target_fine_rules=4_000_000)
+    levels = [grammar.compile_level(c, "viterbi"), grammar.compile_level(f, "viterbi")]
+    path = os.path.join(tempfile.gettempdir(), f"puck_bench_long_{os.getpid()}.grz")
+    grz.write_sequence(path, levels)
+    sents = synth.uniform_sentences(seed, n_sent, 41, 100, len(f.words))
+    log(f"long workload ready in {time.time() - t0:.1f}s: fine nt={levels[1].n_nt} t={levels[1].n_t} "
         f"rules={f.bin_rules.shape[0]} sentences={n_sent} mean_len={np.mean([len(s) for s in sents]):.2f}")
     return levels, path, sents
 
@@ -399,6 +416,130 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_mbr(args):
+    """Sum-product cascade with max-constituent (MBR) trees: throughput of the
+    FP32 CUDA-core path, and its log-partition and posterior errors against
+    the FP64 oracle on a subset."""
+    import numpy as np
+    import torch
+    import oracle
+    from puck_gb300.parser import CLParser, pack_sentences
+    torch.cuda.set_device(0)
+    levels, path, sents = workload(args.seed, args.sentences, fine_semiring="real")
+    words, offsets, _ = pack_sentences(sents)
+    P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, max_length=MAX_LEN, decode="mbr")
+    for _ in range(args.warmup):
+        nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all()
+    dev_ms, api_ms = [], []
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            P.parse_ids(words, offsets)
+            api_ms.append(1e3 * (time.perf_counter() - t0))
+            dev_ms.append(P.stats()["ms_device"])
+    passes = {f"level{l}": [round(v, 2) for v in P.pass_ms(l)[0]] for l in range(len(levels))}
+    # errors on a subset, one batch, against FP64 with the GPU's own masks
+    sub = sents[:args.fp64_subset]
+    w2, o2, lens = pack_sentences(sub)
+    z, st = P.partitions_ids(w2, o2)
+    assert (st == 0).all()
+    nodes, st = P.parse_ids(w2, o2)
+    masks = P.debug_copy(0, "masks")
+    isc, osc = P.debug_copy(0, "iscale"), P.debug_copy(0, "oscale")
+    mbr = P.debug_copy(1, "mbr")
+    P.release()
+    t0 = time.time()
+    r64 = oracle.OracleRun([oracle.OracleLevel(l) for l in levels], sub, precision=64)
+    r64.set_final_masks(masks, isc, osc)
+    assert r64.run("parse") == 0
+    log(f"FP64 oracle on {len(sub)} sentences: {time.time() - t0:.1f}s")
+    ins = r64.chart(1, "inside")
+    pscale = r64.partition_scales(1)
+    cell_off = r64.cell_off
+    root = levels[1].root
+    z64 = np.empty(len(sub))
+    for i, n in enumerate(lens):
+        n = int(n)
+        top_root = cell_off[i] + n * (n + 1) // 2 + (n - 1) * n - (n - 1) * (n - 2) // 2
+        z64[i] = np.log(ins[top_root, root]) + float(isc[top_root]) + pscale[i]
+    rel = np.abs(z.astype(np.float64) - z64) / np.abs(z64)
+    s64, y64 = r64.mbr_cells()
+    sg = mbr[:, 0].astype(np.float64)
+    yg = mbr[:, 1].view(np.int32)
+    live = s64 > 0
+    post_err = np.abs(sg[live] - s64[live]) / np.maximum(np.abs(s64[live]), 1e-30)
+    ref_nodes = r64.trees()
+    same_tree = np.mean([np.array_equal(a[:, :3], b[:, :3]) for a, b in
+                         zip(_blocks(nodes, lens), _blocks(ref_nodes, lens))])
+    value = args.sentences * len(dev_ms) / (sum(dev_ms) / 1e3)
+    out = {
+        "metric": "MBR sentences/sec, 1.1k-symbol split grammar, sum-product (Real) fine level, len<=40",
+        "value": round(value, 2), "unit": "sentences/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(sum(dev_ms) / len(dev_ms), 3), "higher_is_better": True,
+        "dtype": "f32", "data": "synthetic (seeded split grammar and sentences with the published shapes)",
+        "config": {"workload": "split-grammar cascade: coarse Viterbi, masks at -9, fine Real inside/outside, "
+                               f"MBR trees; {args.sentences} sentences lognormal(mean 23) clipped 1-40",
+                   "path": "FP32 CUDA cores (pair-factored sum-product)"},
+        "e2e": {"value": round(args.sentences * len(api_ms) / (sum(api_ms) / 1e3), 2), "unit": "sentences/s"},
+        "clocks": clk.summary(), "passes_ms_last_step": passes,
+        "errors_vs_fp64": {
+            "sentences": len(sub),
+            "log_z_rel_max": float(rel.max()), "log_z_rel_median": float(np.median(rel)),
+            "posterior_rel_max": float(post_err.max()), "posterior_rel_median": float(np.median(post_err)),
+            "best_symbol_agreement": float(np.mean(yg[live] == y64[live])),
+            "mbr_trees_identical": float(same_tree),
+            "cells_compared": int(live.sum()),
+            "note": "posterior = per-cell best coarse marginal (the MBR decode input), cells with a non-zero "
+                    "FP64 marginal; FP64 oracle uses the GPU's coarse masks and scales"},
+    }
+    print(json.dumps(out), flush=True)
+    os.unlink(path)
+
+
+def _blocks(nodes, lens):
+    out, start = [], 0
+    for n in lens:
+        k = max(2 * int(n) - 1, 0)
+        out.append(nodes[start:start + k])
+        start += k
+    return out
+
+
+def run_long(args):
+    """Long sentences (41-100 words) on a ~2,000-symbol grammar: Viterbi
+    cascade throughput per pruning threshold."""
+    import torch
+    from puck_gb300.parser import CLParser, pack_sentences
+    torch.cuda.set_device(0)
+    levels, path, sents = long_workload(args.seed, args.long_sentences)
+    words, offsets, _ = pack_sentences(sents)
+    rows = []
+    for thr in (-6.0, -9.0, -12.0):
+        P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, max_length=100, prune_threshold=thr)
+        nodes, st = P.parse_ids(words, offsets)  # warm-up
+        assert (st == 0).all()
+        t0 = time.perf_counter()
+        P.parse_ids(words, offsets)
+        api = time.perf_counter() - t0
+        s = P.stats()
+        rows.append({"prune_threshold": thr, "sentences_per_s": round(len(sents) / (s["ms_device"] / 1e3), 2),
+                     "e2e_sentences_per_s": round(len(sents) / api, 2), "batches": int(s["batches"]),
+                     "fine_work_units": P.level_work(1)[0],
+                     "passes_ms": {f"level{l}": [round(v, 1) for v in P.pass_ms(l)[0]] for l in range(2)}})
+        log(f"long, threshold {thr}: {rows[-1]}")
+        P.release()
+    out = {"metric": "sentences/sec, ~2k-symbol split grammar, len 41-100, Viterbi cascade",
+           "unit": "sentences/s", "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+           "config": {"workload": f"{levels[1].n_nt + levels[1].n_t} fine symbols, "
+                                  f"{int(sum(l.shape[0] for l in levels[1].bucket_rules))} binary rules, "
+                                  f"{len(sents)} sentences uniform 41-100"},
+           "thresholds": rows}
+    print(json.dumps(out), flush=True)
+    os.unlink(path)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -413,9 +554,18 @@ def main():
     ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x], default="1000,2000,3000")
     ap.add_argument("--serve-sentences", type=int, default=6000)
     ap.add_argument("--serve-mem-gb", type=int, default=32)
+    ap.add_argument("--config", default="viterbi", choices=["viterbi", "mbr", "long"],
+                    help="viterbi: the headline batched/served Viterbi cascade (default); mbr: sum-product "
+                         "MBR throughput and errors against FP64; long: long sentences on a ~2k-symbol grammar")
+    ap.add_argument("--fp64-subset", type=int, default=500)
+    ap.add_argument("--long-sentences", type=int, default=1000)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "mbr":
+        run_mbr(args)
+    elif args.config == "long":
+        run_long(args)
     else:
         run_ours(args)
 

@@ -272,8 +272,10 @@ __global__ void k_root_scores(DevLevel L, DevBatch B, DevWork W, DevMask M, cons
 }
 
 template <class K>
-void set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+cudaError_t set_smem(K kernel, size_t bytes) {
+  // static + dynamic shared memory above 48 KB needs the opt-in, whatever
+  // the dynamic part alone is
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 }  // namespace
@@ -298,7 +300,7 @@ cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const DevWork& 
                            DevNode* nodes, cudaStream_t st) {
   if (W.nent == 0) return cudaSuccess;
   const size_t smem = (size_t)(2 * max_len - 1) * sizeof(DevNode);
-  set_smem(k_viterbi, smem);
+  if (cudaError_t e = set_smem(k_viterbi, smem); e != cudaSuccess) return e;
   k_viterbi<<<W.nent, kVitThreads, smem, st>>>(L, B, W, max_len, inside, nodes);
   return cudaGetLastError();
 }

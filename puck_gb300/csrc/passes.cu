@@ -52,6 +52,7 @@ struct CellCtx {
   int flag0, flag1;
   int g, G;   // this CTA is part g of the cell's G parts
   int last;
+  int wcnt[kThreads / 32];
   unsigned long long work, corner;
 };
 
@@ -238,11 +239,20 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
           live = hit;
         }
       }
+      // the list keeps pair order (a prefix over warps, not an atomic
+      // counter): the parts of a split cell index the same list
       const unsigned bal = __ballot_sync(kFull, live);
-      int wb = 0;
-      if (lane == 0 && bal) wb = atomicAdd(&X.nlive, __popc(bal));
-      wb = __shfl_sync(kFull, wb, 0);
+      if (lane == 0) X.wcnt[warp] = __popc(bal);
+      __syncthreads();
+      int wb = X.nlive, total = 0;
+      for (int w = 0; w < nwarps; ++w) {
+        const int c = X.wcnt[w];
+        wb += w < warp ? c : 0;
+        total += c;
+      }
       if (live) sm.list[wb + __popc(bal & ((1u << lane) - 1u))] = k;
+      __syncthreads();  // every thread has read X.nlive and X.wcnt
+      if (threadIdx.x == 0) X.nlive += total;
     }
     __syncthreads();
     const int nlive = X.nlive;
@@ -668,8 +678,10 @@ __global__ void k_lexicon(DevLevel L, DevBatch B, DevWork W, DevMask M, float* i
 }
 
 template <class K>
-void set_smem(K kernel, size_t bytes) {
-  if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+cudaError_t set_smem(K kernel, size_t bytes) {
+  // static + dynamic shared memory above 48 KB needs the opt-in, whatever
+  // the dynamic part alone is
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 }  // namespace
@@ -717,10 +729,10 @@ cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, 
   const size_t smem = pass_smem_bytes(L, chunk);
   const unsigned grid = (unsigned)W.nunits;
   if (inside_pass) {
-    set_smem(k_inside_span<S, MODE>, smem);
+    if (cudaError_t e = set_smem(k_inside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_inside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside, V, C, chunk);
   } else {
-    set_smem(k_outside_span<S, MODE>, smem);
+    if (cudaError_t e = set_smem(k_outside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_outside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside_c, outside, V, C, chunk);
   }
   return cudaGetLastError();

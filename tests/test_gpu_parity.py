@@ -85,6 +85,41 @@ def test_cascade_masks_charts_trees_bit_exact(size):
     assert pops < 0.8 * levels[0].n_coarse
 
 
+def test_wide_grammar_split_cells_bit_exact():
+    """Hundreds of live coarse pairs per cell and few cells per span launch,
+    so long cells run as several CTAs that must share one pair order."""
+    levels = split_levels("viterbi", "wide")
+    sents = split_sentences(24, seed=31, n_words=400, mean=24, hi=40)
+    P = gpu(levels, "split_wide")
+    words, offsets, _ = pack_sentences(sents)
+    nodes, status = P.parse_ids(words, offsets)
+    assert (status == 0).all()
+    r = oracle.run(levels, sents, mode="parse")
+    assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
+    assert np.array_equal(nodes, r.trees())
+
+
+def test_wide_grammar_real_split_cells_vs_fp64():
+    levels = split_levels("real", "wide")
+    sents = split_sentences(24, seed=32, n_words=400, mean=24, hi=40)
+    P = gpu(levels, "split_wide_real")
+    words, offsets, _ = pack_sentences(sents)
+    z, st = P.partitions_ids(words, offsets)
+    assert (st == 0).all()
+    r32 = oracle.run(levels, sents, mode="partitions")
+    masks, isc, osc = r32.masks(0)
+    r64 = oracle.OracleRun([oracle.OracleLevel(l) for l in levels], sents, precision=64)
+    r64.set_final_masks(masks, isc, osc)
+    assert r64.run("partitions") == 0
+    z64 = r64.partitions().astype(np.float64)
+    rel = np.abs(z.astype(np.float64) - z64) / np.abs(z64)
+    assert rel.max() < LOGZ_RTOL, rel.max()
+    # the inside chart agrees with the FP32 oracle to rounding
+    gi, oi = P.debug_copy(1, "inside"), r32.chart(1, "inside")
+    nz = np.abs(oi) > 1e-30
+    assert np.median(np.abs(gi - oi)[nz] / np.abs(oi)[nz]) < 1e-5
+
+
 def test_batching_does_not_change_results():
     levels = split_levels("viterbi", "medium")
     sents = split_sentences(40, seed=9)
