@@ -468,8 +468,12 @@ def run_mbr(args):
     s64, y64 = r64.mbr_cells()
     sg = mbr[:, 0].astype(np.float64)
     yg = mbr[:, 1].view(np.int32)
-    live = s64 > 0
-    post_err = np.abs(sg[live] - s64[live]) / np.maximum(np.abs(s64[live]), 1e-30)
+    # cells whose FP64 best marginal is a normal FP32 number (the FP32 path
+    # cannot represent smaller values to full precision)
+    live = s64 > 1.2e-38
+    nonfinite = int((~np.isfinite(sg[live])).sum())
+    ok = live & np.isfinite(sg)
+    post_err = np.abs(sg[ok] - s64[ok]) / np.abs(s64[ok])
     ref_nodes = r64.trees()
     same_tree = np.mean([np.array_equal(a[:, :3], b[:, :3]) for a, b in
                          zip(_blocks(nodes, lens), _blocks(ref_nodes, lens))])
@@ -488,11 +492,13 @@ def run_mbr(args):
             "sentences": len(sub),
             "log_z_rel_max": float(rel.max()), "log_z_rel_median": float(np.median(rel)),
             "posterior_rel_max": float(post_err.max()), "posterior_rel_median": float(np.median(post_err)),
+            "posterior_nonfinite_cells": nonfinite,
             "best_symbol_agreement": float(np.mean(yg[live] == y64[live])),
             "mbr_trees_identical": float(same_tree),
             "cells_compared": int(live.sum()),
-            "note": "posterior = per-cell best coarse marginal (the MBR decode input), cells with a non-zero "
-                    "FP64 marginal; FP64 oracle uses the GPU's coarse masks and scales"},
+            "note": "posterior = per-cell best coarse marginal (the MBR decode input), over cells whose FP64 "
+                    "marginal is at least the smallest normal FP32 number; the FP64 oracle uses the GPU's "
+                    "coarse masks and scales"},
     }
     print(json.dumps(out), flush=True)
     os.unlink(path)
