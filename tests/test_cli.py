@@ -1,0 +1,143 @@
+"""The command-line front ends (compile_grammar, run_parser) and the
+Berkeley text-grammar reader.
+
+The reader is checked on the reference's own text grammars when they are
+present on this machine; its parity with epic's reader is unpinned.
+"""
+import io
+import os
+import subprocess
+import sys
+from concurrent.futures import Future
+
+import numpy as np
+import pytest
+
+import oracle
+from puck_gb300 import berkeley, compile_grammar, grammar, grz, run_parser
+from puck_gb300.parser import CLParserData, Failure, Success, Tree, nodes_to_viterbi_tree
+
+TEXT = "/root/reference/textGrammars"
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_parse_mem_matches_reference_suffixes():
+    assert run_parser.parse_mem("3g") == 3 << 30
+    assert run_parser.parse_mem("512m") == 512 << 20
+    assert run_parser.parse_mem("100") == 100
+    with pytest.raises(Exception):
+        run_parser.parse_mem("lots")
+
+
+def test_fine_semiring_flags():
+    assert compile_grammar.fine_semiring(True, False) == "viterbi"
+    assert compile_grammar.fine_semiring(True, True) == "viterbi"
+    assert compile_grammar.fine_semiring(False, True) == "logsum"
+    assert compile_grammar.fine_semiring(False, False) == "real"
+
+
+def test_compile_grammar_synthetic_writes_a_loadable_archive(tmp_path):
+    out = str(tmp_path / "g.grz")
+    assert compile_grammar.main(["--synthetic", "pcfg", "--seed", "0", "--grammar", out, "--viterbi", "false"]) == 0
+    levels = grz.read_sequence(out)
+    assert len(levels) == 1 and not levels[0].is_viterbi
+
+
+def test_compile_grammar_refuses_reproject(tmp_path):
+    assert compile_grammar.main(["--synthetic", "pcfg", "--grammar", str(tmp_path / "g.grz"),
+                                 "--reproject"]) == 2
+
+
+class _FakeServer:
+    """Completes every sentence with a one-node-per-word flat tree, or with a
+    failure for sentences containing 'BAD'."""
+
+    def submit(self, words):
+        f = Future()
+        if "BAD" in words:
+            f.set_result(Failure("OOV"))
+        else:
+            kids = [Tree("T", [], i, i + 1) for i in range(len(words))]
+            f.set_result(Success(Tree("ROOT", kids, 0, len(words))))
+        return f
+
+
+def test_run_parser_stream_order_and_failure_policy():
+    src = io.StringIO("a b c\n\n  \nx BAD y\n" + " ".join(["w"] * 7) + "\nd e\n")
+    sink = io.StringIO()
+    n = run_parser.parse_stream(_FakeServer(), src, sink, max_length=7, window=2)
+    assert n == 4  # blank lines are skipped
+    lines = sink.getvalue().splitlines()
+    assert lines == ["(ROOT (T a) (T b) (T c))", "(())", "(())", "(ROOT (T d) (T e))"]
+
+
+@pytest.mark.skipif(not os.path.exists(TEXT + "/wsj_1.gr.binary"), reason="reference text grammars absent")
+def test_berkeley_reader_on_reference_grammars():
+    g0, g1 = berkeley.read_cascade([TEXT + "/wsj_0.gr", TEXT + "/wsj_1.gr"])
+    assert g0.coarse_names == g1.coarse_names and g0.words == g1.words
+    # every substate of wsj_1 projects onto its base label
+    for lab, c in zip(g1.labels, g1.coarse):
+        assert lab.rsplit("_", 1)[0] == g1.coarse_names[c]
+    # identity unaries exist for every nonterminal
+    l1 = grammar.compile_level(g1, "viterbi")
+    ident = {(int(p), int(c)) for p, c in g1.un_rules if p == c}
+    assert all((int(x), int(x)) in ident for x in l1.nt_labels)
+    # the lexicon keeps one entry per substate with a positive probability
+    assert g1.lex_label.shape[0] > g0.lex_label.shape[0]
+    assert np.all(g1.lex_score <= 0)
+
+
+@pytest.mark.skipif(not os.path.exists(TEXT + "/wsj_1.gr.binary"), reason="reference text grammars absent")
+def test_berkeley_cascade_parses_english_on_the_oracle(tmp_path):
+    gs = berkeley.read_cascade([TEXT + "/wsj_0.gr", TEXT + "/wsj_1.gr"])
+    levels = [grammar.compile_level(gs[0], "viterbi"), grammar.compile_level(gs[1], "viterbi")]
+    wid = {w: i for i, w in enumerate(gs[1].words)}
+    text = ["The company said it expects revenue to rise .", "He sold shares of the stock ."]
+    sents = [np.array([wid[w] for w in s.split()], np.int32) for s in text]
+    r = oracle.run(levels, sents, mode="parse")
+    nodes = r.trees()
+    path = str(tmp_path / "wsj.grz")
+    grz.write_sequence(path, levels)
+    data = CLParserData.read_sequence(path)[-1]
+    first = nodes_to_viterbi_tree(nodes[:2 * len(sents[0]) - 1], data)
+    assert first.label == "ROOT"
+    assert np.isfinite(nodes[0, 3].view(np.float32))
+    assert first.preterminal_labels()[-1] == "."
+
+
+def _module(mod, *args, **kw):
+    return subprocess.run([sys.executable, "-m", mod, *args], cwd=ROOT, capture_output=True, text=True,
+                          timeout=600, **kw)
+
+
+def test_cli_help_runs():
+    for mod in ("puck_gb300.run_parser", "puck_gb300.compile_grammar"):
+        r = _module(mod, "--help")
+        assert r.returncode == 0 and "--grammar" in r.stdout
+
+
+@pytest.mark.gpu
+def test_run_parser_end_to_end_matches_oracle(tmp_path):
+    from puck_gb300 import synth
+    out = str(tmp_path / "g.grz")
+    assert compile_grammar.main(["--synthetic", "pcfg", "--seed", "0", "--grammar", out]) == 0
+    g = synth.small_pcfg(0)
+    sents = synth.uniform_sentences(5, 12, 5, 20, 5000)
+    text = [" ".join(g.words[i] for i in s) for s in sents]
+    text[3] = text[3] + " not_a_word"
+    inp = tmp_path / "in.txt"
+    inp.write_text("\n".join(text) + "\n")
+    r = _module("puck_gb300.run_parser", "--grammar", out, "--maxLength", "19", "--mem", "2g", str(inp))
+    assert r.returncode == 0, r.stderr
+    lines = (tmp_path / "in.txt.parsed").read_text().splitlines()
+    assert len(lines) == len(text)
+    levels = [grammar.compile_level(g, "viterbi")]
+    data = CLParserData.read_sequence(out)[-1]
+    from puck_gb300.parser import debinarize
+    for i, s in enumerate(sents):
+        words = text[i].split()
+        if i == 3 or len(words) >= 19:
+            assert lines[i] == "(())"
+            continue
+        ref = oracle.run(levels, [s], mode="parse").trees()
+        assert lines[i] == debinarize(nodes_to_viterbi_tree(ref, data)).render(words)
