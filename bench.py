@@ -292,7 +292,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     levels, path, sents = workload(args.seed + rank, args.sentences)
     words, offsets, lens = pack_sentences(sents)
-    P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, device=local, max_length=MAX_LEN)
+    P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, device=local, max_length=MAX_LEN,
+                 use_graphs=True)
     for _ in range(args.warmup):
         nodes, st = P.parse_ids(words, offsets)
     assert (st == 0).all(), "sentences failed to parse"

@@ -423,6 +423,10 @@ struct puck_parser {
   std::vector<std::array<double, 4>> pass_ms;
   std::vector<std::array<int64_t, 4>> pass_launches;
   std::vector<std::array<int64_t, 2>> level_work;  // per level: work units, +0.0 partials (last call)
+  // use_graphs: per level, the executable graphs of the inside and outside
+  // span sequences, updated in place while a new batch keeps their shape
+  std::vector<std::array<cudaGraphExec_t, 2>> graphs;
+  int64_t graph_updates = 0, graph_instantiations = 0;
 };
 
 namespace {
@@ -440,6 +444,52 @@ int64_t bytes_per_cell(const puck_parser* P, Mode mode) {
     else b += 8;
   }
   return b;
+}
+
+// Runs `issue` (which enqueues kernels on st) directly, or, with use_graphs,
+// captures it into a graph and launches that graph.  The executable graph of
+// (level, pass) is kept and updated in place when the next batch has the
+// same launch sequence; grid sizes and kernel arguments may differ.
+template <class F>
+void launch_sequence(puck_parser* P, int level, int pass, cudaStream_t st, F&& issue) {
+  if (!P->opt.use_graphs) {
+    issue();
+    return;
+  }
+  cudaGraph_t g = nullptr;
+  CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+  try {
+    issue();
+  } catch (...) {
+    cudaStreamEndCapture(st, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  CUDA_TRY(cudaStreamEndCapture(st, &g));
+  cudaGraphExec_t& ex = P->graphs[level][pass];
+  bool updated = false;
+  if (ex) {
+    cudaGraphExecUpdateResultInfo info{};
+    updated = cudaGraphExecUpdate(ex, g, &info) == cudaSuccess;
+    if (!updated) {
+      cudaGetLastError();  // clear the failed update
+      cudaGraphExecDestroy(ex);
+      ex = nullptr;
+    }
+  }
+  if (!ex) {
+    const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+    if (e != cudaSuccess) {
+      cudaGraphDestroy(g);
+      ex = nullptr;
+      CUDA_TRY(e);
+    }
+    ++P->graph_instantiations;
+  } else {
+    ++P->graph_updates;
+  }
+  cudaGraphDestroy(g);
+  CUDA_TRY(cudaGraphLaunch(ex, st));
 }
 
 struct BatchPlan {
@@ -582,19 +632,23 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     rec(EV[0]);
     const puck::Counters C{P->b_counters.as<unsigned long long>() + 2 * l,
                            P->b_counters.as<unsigned long long>() + 2 * l + 1, P->b_status.as<int>()};
-    CUDA_TRY(puck::launch_lexicon(D, B, Wtok, MM, inside, lb.part.as<double>(), V, C, st));
-    ++LC[0];
-    for (int span = 1; span <= max_len; ++span) {
-      CUDA_TRY(puck::launch_inside_span(D, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
+    launch_sequence(P, l, 0, st, [&] {
+      CUDA_TRY(puck::launch_lexicon(D, B, Wtok, MM, inside, lb.part.as<double>(), V, C, st));
       ++LC[0];
-    }
+      for (int span = 1; span <= max_len; ++span) {
+        CUDA_TRY(puck::launch_inside_span(D, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
+        ++LC[0];
+      }
+    });
     rec(EV[1]);
     if (need_out) {
-      for (int span = max_len; span >= 1; --span) {
-        CUDA_TRY(puck::launch_outside_span(D, B, work(span_list[span], span), MM, max_len, inside, outside, V, C,
-                                           st));
-        ++LC[1];
-      }
+      launch_sequence(P, l, 1, st, [&] {
+        for (int span = max_len; span >= 1; --span) {
+          CUDA_TRY(puck::launch_outside_span(D, B, work(span_list[span], span), MM, max_len, inside, outside, V,
+                                             C, st));
+          ++LC[1];
+        }
+      });
     }
     rec(EV[2]);
     if (!last) {
@@ -870,6 +924,7 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
     P->pass_ms.assign(nl, std::array<double, 4>{0, 0, 0, 0});
     P->pass_launches.assign(nl, std::array<int64_t, 4>{0, 0, 0, 0});
     P->level_work.assign(nl, std::array<int64_t, 2>{0, 0});
+    P->graphs.assign(nl, std::array<cudaGraphExec_t, 2>{nullptr, nullptr});
     for (int l = 0; l < nl; ++l) {
       P->levels.emplace_back(new LevelDev());
       build_level(*P->levels.back(), g->levels[l], l < nl - 1 && nl != 1);
@@ -899,6 +954,9 @@ void puck_parser_destroy(puck_parser* P) {
   for (DevBuf* b : {&P->b_len, &P->b_cell_off, &P->b_word_off, &P->b_words, &P->b_work, &P->b_node_off, &P->b_mbr_off, &P->b_nodes, &P->b_status,
                     &P->b_logz, &P->b_scratch, &P->b_counters, &P->b_parts, &P->b_cell_cnt})
     b->release();
+  for (auto& a : P->graphs)
+    for (auto& ex : a)
+      if (ex) cudaGraphExecDestroy(ex);
   P->levels.clear();
   for (auto& e : P->ev_batch)
     if (e) cudaEventDestroy(e);

@@ -186,7 +186,7 @@ class CLParser:
 
     def __init__(self, grammar_path: str, max_alloc_size: int = 1 << 30, profile: bool = False,
                  device: int = 0, decode: str = "auto", max_length: int = 100,
-                 prune_threshold: float = -9.0, max_batch_sentences: int = 0):
+                 prune_threshold: float = -9.0, max_batch_sentences: int = 0, use_graphs: bool = False):
         L = _lib.load()
         st = ctypes.c_int32(0)
         self._g = L.puck_grammar_load(grammar_path.encode(), ctypes.byref(st))
@@ -202,6 +202,7 @@ class CLParser:
         opt.max_length = max_length
         opt.prune_threshold = prune_threshold
         opt.max_batch_sentences = max_batch_sentences
+        opt.use_graphs = 1 if use_graphs else 0
         self.max_length = max_length
         self._p = L.puck_parser_create(self._g, ctypes.byref(opt), ctypes.byref(st))
         if not self._p:

@@ -120,6 +120,25 @@ def test_wide_grammar_real_split_cells_vs_fp64():
     assert np.median(np.abs(gi - oi)[nz] / np.abs(oi)[nz]) < 1e-5
 
 
+def test_graph_capture_gives_identical_results():
+    """use_graphs: span sequences captured and replayed as CUDA graphs, the
+    second and third calls updating the kept graphs in place."""
+    levels = split_levels("viterbi", "small")
+    sents = split_sentences(40, seed=41, n_words=300, mean=12, hi=30)
+    words, offsets, _ = pack_sentences(sents)
+    ref, _ = gpu(levels, "split_small").parse_ids(words, offsets)
+    G = gpu(levels, "split_small", use_graphs=True)
+    for _ in range(3):
+        nodes, st = G.parse_ids(words, offsets)
+        assert (st == 0).all()
+        assert np.array_equal(nodes, ref)
+    # a batch with another shape re-captures
+    w2, o2, _ = pack_sentences(sents[:17])
+    n2, _ = G.parse_ids(w2, o2)
+    r2, _ = gpu(levels, "split_small").parse_ids(w2, o2)
+    assert np.array_equal(n2, r2)
+
+
 def test_batching_does_not_change_results():
     levels = split_levels("viterbi", "medium")
     sents = split_sentences(40, seed=9)
