@@ -303,13 +303,13 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       const int bk1 = __ldg(J.pair_blk + p + 1);
       for (int bk = __ldg(J.pair_blk + p); bk < bk1; ++bk) {
         if (gated && !gate_hit(J, __ldg(J.blk_seg + bk), ms, L.gate_merged, X.gate)) continue;
-        const int r0 = __ldg(J.blk_ptr + bk), r1 = __ldg(J.blk_ptr + bk + 1);
-        const int per = (r1 - r0 + 31) >> 5;
-        const int rs = r0 + lane * per, re = min(r1, rs + per);
+        // lane l runs its contiguous, target-sorted slice of the block; the
+        // slices are stored interleaved, so each step's loads are coalesced
+        const int r0 = __ldg(J.blk_ptr + bk), per = (__ldg(J.blk_ptr + bk + 1) - r0) >> 5;
         int cur = -1;
         float run = Sr<S>::zero();
-        for (int r = rs; r < re; ++r) {
-          const int2 R = __ldg(J.pair_rules + r);
+        for (int i = 0; i < per; ++i) {
+          const int2 R = __ldg(J.pair_rules + r0 + i * 32 + lane);
           const int j = R.x & 255, k = (R.x >> 8) & 255, t = (int)((unsigned)R.x >> 16);
           const float w = __int_as_float(R.y);
           const float v = S == SEMI_VITERBI ? Mw[j * nz + k] + w : Mw[j * nz + k] * w;
@@ -322,7 +322,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
           }
         }
         if (cur >= 0) flush_run<S>(P, cur, run, corner);
-        if (lane == 0) work += (unsigned long long)(r1 - r0);
+        if (lane == 0) work += (unsigned long long)__ldg(J.blk_nrule + bk);
       }
       __syncwarp();
     }

@@ -39,7 +39,8 @@ struct DevJob {
   const int* pair_gate;   // [npair * mask_size] OR of the pair's segment bits
   const int* pair_blk;    // [npair + 1] block range
   const int* blk_seg;     // [nblk]
-  const int* blk_ptr;     // [nblk + 1] rule range
+  const int* blk_ptr;     // [nblk + 1] rule range, each a multiple of 32 (lane-interleaved, padded)
+  const int* blk_nrule;   // [nblk] rules of the block before padding
   const int2* pair_rules;
 };
 

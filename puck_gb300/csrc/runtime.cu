@@ -332,15 +332,39 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.nseg = (int)(nseg / std::max(1, L.mask_size));
     static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
     static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
-    int64_t npk = 0, nr = 0;
+    int64_t npk = 0, nr = 0, nbp = 0;
     const int* pk = L.get<int>(n + "/pair_key", "i4", &npk);
     const int* pr = L.get<int>(n + "/pair_rule", "i4", &nr);
     const float* pw = L.get<float>(n + "/pair_w", "f4", nullptr);
-    std::vector<int2> rr(nr);
-    for (int64_t k = 0; k < nr; ++k) {
-      rr[k].x = pr[k];
-      std::memcpy(&rr[k].y, &pw[k], 4);
+    const int* bp = L.get<int>(n + "/blk_ptr", "i4", &nbp);
+    // Device layout of a block's rules: padded to a multiple of 32 and
+    // interleaved, so that lane l's contiguous slice [l*per, (l+1)*per) is
+    // read as rules[i*32 + l], i = 0..per-1 (coalesced across the warp).
+    // Padding rules carry the semiring zero as weight and the block's last
+    // target, so they never change a cell.
+    const float zero = L.semiring == puck::SEMI_REAL ? 0.f : -INFINITY;
+    std::vector<int2> rr;
+    std::vector<int> dev_bp(1, 0), blk_n;
+    for (int64_t b = 0; b + 1 < nbp; ++b) {
+      const int r0 = bp[b], cnt = bp[b + 1] - bp[b], per = (cnt + 31) / 32;
+      const size_t base = rr.size();
+      rr.resize(base + (size_t)per * 32);
+      for (int slot = 0; slot < per * 32; ++slot) {
+        const int lane = slot % 32, i = slot / 32, logical = lane * per + i;
+        int2 v;
+        if (logical < cnt) {
+          v.x = pr[r0 + logical];
+          std::memcpy(&v.y, &pw[r0 + logical], 4);
+        } else {
+          v.x = cnt ? (pr[r0 + cnt - 1] & ~0xffff) : 0;  // target kept, operands (0, 0)
+          std::memcpy(&v.y, &zero, 4);
+        }
+        rr[base + slot] = v;
+      }
+      dev_bp.push_back((int)rr.size());
+      blk_n.push_back(cnt);
     }
+    if (rr.size() > (size_t)INT32_MAX) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule table too large in " + n};
     J.npair = (int)npk;
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];
@@ -348,7 +372,8 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
     J.pair_blk = up<int>(D, L, n + "/pair_blk", "i4");
     J.blk_seg = up<int>(D, L, n + "/blk_seg", "i4");
-    J.blk_ptr = up<int>(D, L, n + "/blk_ptr", "i4");
+    J.blk_ptr = static_cast<const int*>(D.upload(dev_bp.data(), dev_bp.size() * sizeof(int)));
+    J.blk_nrule = static_cast<const int*>(D.upload(blk_n.data(), std::max<size_t>(blk_n.size(), 1) * sizeof(int)));
     J.pair_rules = reinterpret_cast<const int2*>(D.upload(rr.data(), rr.size() * sizeof(int2)));
     d.max_npair = std::max(d.max_npair, J.npair);
     const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
