@@ -156,6 +156,8 @@ struct Finishing {
   int64_t id;
   long long node_at;
   int n;
+  int slot;
+  long long cell_off;
 };
 
 // Host and device buffers of one tick in flight.
@@ -167,6 +169,10 @@ struct TickBuf {
   puck::DevNode* out_dev = nullptr;
   size_t out_cap = 0;  // nodes
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr;
+  // the decode runs on its own stream once the last level's passes of the
+  // tick are done, overlapping the next ticks
+  cudaEvent_t ev_fine = nullptr, ev_dec_begin = nullptr, ev_dec_end = nullptr;
+  bool decoded = false;
   std::vector<cudaEvent_t> ev_group;  // profile: after the slot update, then after each step group
   std::vector<Finishing> finishing;
   int64_t launches = 0, h2d = 0, d2h = 0;
@@ -198,7 +204,7 @@ struct puck_server {
   puck_options opt{};
   int nl = 0;
   bool mbr = false;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr, dstream = nullptr;
   std::vector<std::unique_ptr<LevelDev>> levels;
   std::vector<LevelArena> la;
   DevBuf d_len, d_cell_off, d_node_off, d_mbr_off, d_words, d_status, d_counters, d_decode, d_scratch, d_parts,
@@ -311,24 +317,29 @@ void fail_all(puck_server* S, puck_status st) {
 void harvest(puck_server* S, int p) {
   TickBuf& T = S->tb[p];
   CUDA_TRY(cudaEventSynchronize(T.ev_end));
-  float ms = 0.f;
+  float ms = 0.f, dms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, T.ev_begin, T.ev_end));
+  if (T.decoded) {
+    CUDA_TRY(cudaEventSynchronize(T.ev_dec_end));
+    CUDA_TRY(cudaEventElapsedTime(&dms, T.ev_dec_begin, T.ev_dec_end));
+  }
   std::vector<float> gms(T.ev_group.size() > 1 ? T.ev_group.size() - 1 : 0, 0.f);
   for (size_t k = 0; k < gms.size(); ++k) CUDA_TRY(cudaEventElapsedTime(&gms[k], T.ev_group[k], T.ev_group[k + 1]));
   const int64_t t = now_ns();
   std::lock_guard<std::mutex> lk(S->mu);
-  for (size_t k = 0; k < gms.size(); ++k) {
-    const int level = std::min<int>((int)k / 4, S->nl - 1), kind = (int)k < 4 * S->nl ? (int)k % 4 : 4;
-    S->pass_ms[level][kind] += gms[k];
-  }
+  for (size_t k = 0; k < gms.size(); ++k) S->pass_ms[k / 4][k % 4] += gms[k];
+  if (!T.ev_group.empty()) S->pass_ms[S->nl - 1][4] += dms;
   for (const Finishing& f : T.finishing) {
     Request& r = S->reqs[f.id];
     r.nodes.assign(T.out_host + f.node_at, T.out_host + f.node_at + (2 * f.n - 1));
     r.t_done = t;
     S->done_q.push_back(f.id);
     ++S->stats.completed;
+    // the decode has read the sentence's cells: they and its slot are free
+    S->arena.release(f.cell_off, 2 * tri(f.n));
+    S->free_slots.push_back(f.slot);
   }
-  S->stats.ms_device += ms;
+  S->stats.ms_device += ms + dms;
   S->stats.kernel_launches += T.launches;
   S->stats.h2d_bytes += T.h2d;
   S->stats.d2h_bytes += T.d2h;
@@ -374,8 +385,6 @@ bool run_tick(puck_server* S, int p) {
   long long out_nodes = 0;
   std::vector<Resident> keep;
   keep.reserve(S->resident.size());
-  std::vector<std::pair<long long, long long>> freed_cells;
-  std::vector<int> freed_slots;
   for (Resident r : S->resident) {
     int last_g = -1;
     bool done = false;
@@ -388,14 +397,12 @@ bool run_tick(puck_server* S, int p) {
       L.pref.push_back((int)units_of(r));  // per-entry units; prefix formed below
       last_g = g;
       if (r.stage == ST_DEC) {
-        T.finishing.push_back(Finishing{r.id, out_nodes, r.n});
+        T.finishing.push_back(Finishing{r.id, out_nodes, r.n, r.slot, r.cell_off});
         // a sentence admitted in this tick keeps one record (two records of
         // one slot would race in k_slot_update)
         if (r.upd >= 0) upd[r.upd].node_off = out_nodes;
         else upd.push_back(SlotUpdate{r.cell_off, out_nodes, 6 * r.cell_off, r.slot, r.n, -1, 0});
         out_nodes += 2 * r.n - 1;
-        freed_cells.emplace_back(r.cell_off, 2 * tri(r.n));
-        freed_slots.push_back(r.slot);
         done = true;
         break;
       }
@@ -502,12 +509,6 @@ bool run_tick(puck_server* S, int p) {
     CUDA_TRY(cudaGetLastError());
     ++T.launches;
   }
-  // freed ranges and slots become available to sentences admitted next tick
-  {
-    std::lock_guard<std::mutex> lk(S->mu);
-    for (auto& c : freed_cells) S->arena.release(c.first, c.second);
-    for (int s : freed_slots) S->free_slots.push_back(s);
-  }
 
   puck::DevBatch B{};
   B.nsent = S->slots;
@@ -587,22 +588,25 @@ bool run_tick(puck_server* S, int p) {
     }
     mark(4 * l + 4);
     const StepList& Ldec = lists[4 * S->nl];
-    if (Ldec.sent.empty()) {
-      mark(4 * S->nl + 1);
-      continue;
-    }
+    T.decoded = !Ldec.sent.empty();
+    if (!T.decoded) continue;
+    // decode on the side stream, after this tick's last-level passes
+    cudaStream_t ds = S->dstream;
+    CUDA_TRY(cudaEventRecord(T.ev_fine, st));
+    CUDA_TRY(cudaStreamWaitEvent(ds, T.ev_fine, 0));
+    CUDA_TRY(cudaEventRecord(T.ev_dec_begin, ds));
     puck::DevWork W = work(Ldec);
     if (!S->mbr) {
-      CUDA_TRY(puck::launch_viterbi(D, B, W, maxlen, inside, T.out_dev, st));
+      CUDA_TRY(puck::launch_viterbi(D, B, W, maxlen, inside, T.out_dev, ds));
       ++T.launches;
     } else {
-      CUDA_TRY(puck::launch_mbr_cells(D, B, W, inside, outside, S->d_decode.as<float2>(), st));
+      CUDA_TRY(puck::launch_mbr_cells(D, B, W, inside, outside, S->d_decode.as<float2>(), ds));
       W.pref = nullptr;
       CUDA_TRY(puck::launch_mbr_decode(B, W, M, D.semiring == puck::SEMI_REAL ? 1 : 0, S->d_decode.as<float2>(),
-                                       S->d_mbr_off.as<long long>(), S->d_scratch.as<float>(), T.out_dev, st));
+                                       S->d_mbr_off.as<long long>(), S->d_scratch.as<float>(), T.out_dev, ds));
       T.launches += 2;
     }
-    mark(4 * S->nl + 1);
+    CUDA_TRY(cudaEventRecord(T.ev_dec_end, ds));
   }
   CUDA_TRY(cudaEventRecord(T.ev_end, st));
   {
@@ -673,6 +677,8 @@ void destroy_server(puck_server* S) {
     T.dev.release();
     if (T.ev_begin) cudaEventDestroy(T.ev_begin);
     if (T.ev_end) cudaEventDestroy(T.ev_end);
+    for (cudaEvent_t e : {T.ev_fine, T.ev_dec_begin, T.ev_dec_end})
+      if (e) cudaEventDestroy(e);
     for (cudaEvent_t e : T.ev_group) cudaEventDestroy(e);
   }
   for (LevelArena& A : S->la)
@@ -683,6 +689,7 @@ void destroy_server(puck_server* S) {
     b->release();
   S->levels.clear();
   if (S->stream) cudaStreamDestroy(S->stream);
+  if (S->dstream) cudaStreamDestroy(S->dstream);
   delete S;
 }
 
@@ -719,15 +726,19 @@ puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts,
     CUDA_TRY(cudaSetDevice(S->opt.device));
     CUDA_TRY(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->opt.device));
     CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->dstream, cudaStreamNonBlocking));
     for (TickBuf& T : S->tb) {
       CUDA_TRY(cudaEventCreate(&T.ev_begin));
       CUDA_TRY(cudaEventCreate(&T.ev_end));
+      CUDA_TRY(cudaEventCreate(&T.ev_fine));
+      CUDA_TRY(cudaEventCreate(&T.ev_dec_begin));
+      CUDA_TRY(cudaEventCreate(&T.ev_dec_end));
     }
     S->nl = (int)g->levels.size();
     S->pass_ms.assign(S->nl, std::array<double, 5>{0, 0, 0, 0, 0});
     for (TickBuf& T : S->tb) {
       if (!S->opt.profile) continue;
-      T.ev_group.resize(4 * S->nl + 2);
+      T.ev_group.resize(4 * S->nl + 1);
       for (cudaEvent_t& e : T.ev_group) CUDA_TRY(cudaEventCreate(&e));
     }
     for (int l = 0; l < S->nl; ++l) {
