@@ -36,6 +36,7 @@ using namespace dev;
 
 constexpr int kPairChunk = 64;   // splits per liveness chunk (two ballots)
 constexpr int kThreads = 256;
+constexpr int kRuleBatch = 4;   // rules per lane whose loads are in flight together
 
 // Shared bookkeeping of one target cell.
 struct CellCtx {
@@ -277,20 +278,33 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         float acc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q] = Sr<S>::zero();
-        for (unsigned long long mm = m; mm; mm &= mm - 1) {
-          const int s = __ffsll(mm) - 1;
-          const float* A = X.aptr[c0 + s];
-          const float* B = X.bptr[c0 + s];
-          const float a = __ldg(A + ai);
+        // two live splits per step, their loads issued together; an odd last
+        // split is paired with itself (max is idempotent; the Real pass adds
+        // its second term with a zero weight), in the same order as one by one
+        for (unsigned long long mm = m; mm;) {
+          const int s0 = __ffsll(mm) - 1;
+          mm &= mm - 1;
+          const bool two = mm != 0;
+          const int s1 = two ? __ffsll(mm) - 1 : s0;
+          if (two) mm &= mm - 1;
+          const float* A0 = X.aptr[c0 + s0];
+          const float* B0 = X.bptr[c0 + s0];
+          const float* A1 = X.aptr[c0 + s1];
+          const float* B1 = X.bptr[c0 + s1];
+          const float a0v = __ldg(A0 + ai), a1v = __ldg(A1 + ai);
+          float b0v[4], b1v[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            b0v[q] = bi[q] >= 0 ? __ldg(B0 + bi[q]) : 0.f;
+            b1v[q] = bi[q] >= 0 ? __ldg(B1 + bi[q]) : 0.f;
+          }
           if (S == SEMI_VITERBI) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (bi[q] >= 0) acc[q] = fmaxf(acc[q], a + __ldg(B + bi[q]));
+            for (int q = 0; q < 4; ++q) acc[q] = fmaxf(acc[q], fmaxf(a0v + b0v[q], a1v + b1v[q]));
           } else {
-            const float as = a * X.scl[c0 + s];
+            const float as0 = a0v * X.scl[c0 + s0], as1 = two ? a1v * X.scl[c0 + s1] : 0.f;
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (bi[q] >= 0) acc[q] = fmaf(as, __ldg(B + bi[q]), acc[q]);
+            for (int q = 0; q < 4; ++q) acc[q] = fmaf(as1, b1v[q], fmaf(as0, b0v[q], acc[q]));
           }
         }
 #pragma unroll
@@ -308,17 +322,29 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         const int r0 = __ldg(J.blk_ptr + bk), per = (__ldg(J.blk_ptr + bk + 1) - r0) >> 5;
         int cur = -1;
         float run = Sr<S>::zero();
-        for (int i = 0; i < per; ++i) {
-          const int2 R = __ldg(J.pair_rules + r0 + i * 32 + lane);
-          const int j = R.x & 255, k = (R.x >> 8) & 255, t = (int)((unsigned)R.x >> 16);
-          const float w = __int_as_float(R.y);
-          const float v = S == SEMI_VITERBI ? Mw[j * nz + k] + w : Mw[j * nz + k] * w;
-          if (t != cur) {
-            if (cur >= 0) flush_run<S>(P, cur, run, corner);
-            cur = t;
-            run = v;
-          } else {
-            run = Sr<S>::add(run, v);
+        // kRuleBatch rules per step: their loads are issued before any is used
+        // (the step count `per` is the same for every lane of the warp)
+        for (int i0 = 0; i0 < per; i0 += kRuleBatch) {
+          int2 R[kRuleBatch];
+#pragma unroll
+          for (int q = 0; q < kRuleBatch; ++q)
+            R[q] = i0 + q < per ? __ldg(J.pair_rules + r0 + (i0 + q) * 32 + lane) : make_int2(0, 0);
+          float m4[kRuleBatch];
+#pragma unroll
+          for (int q = 0; q < kRuleBatch; ++q) m4[q] = Mw[(R[q].x & 255) * nz + ((R[q].x >> 8) & 255)];
+#pragma unroll
+          for (int q = 0; q < kRuleBatch; ++q) {
+            if (i0 + q >= per) break;
+            const int t = (int)((unsigned)R[q].x >> 16);
+            const float w = __int_as_float(R[q].y);
+            const float v = S == SEMI_VITERBI ? m4[q] + w : m4[q] * w;
+            if (t != cur) {
+              if (cur >= 0) flush_run<S>(P, cur, run, corner);
+              cur = t;
+              run = v;
+            } else {
+              run = Sr<S>::add(run, v);
+            }
           }
         }
         if (cur >= 0) flush_run<S>(P, cur, run, corner);
