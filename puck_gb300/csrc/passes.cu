@@ -448,10 +448,11 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 
 // ---------------------------------------------------------------------------
 // Inside pass over the cells of a work list (span 1: the unary layer over
-// lexicon cells).  Register budgets: five CTAs per SM for the pair-factored
-// mode, six for the target-major mode (the Viterbi instances without spills).
+// lexicon cells).  Register budgets: six CTAs per SM in both modes (the
+// pair-factored Viterbi instance spills 32 bytes there and is still faster
+// than at five CTAs: the kernel is latency-bound).
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
+__global__ void __launch_bounds__(256, 6)
     k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
