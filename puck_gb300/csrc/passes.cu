@@ -331,7 +331,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
             R[q] = i0 + q < per ? __ldg(J.pair_rules + r0 + (i0 + q) * 32 + lane) : make_int2(0, 0);
           float m4[kRuleBatch];
 #pragma unroll
-          for (int q = 0; q < kRuleBatch; ++q) m4[q] = Mw[(R[q].x & 255) * nz + ((R[q].x >> 8) & 255)];
+          for (int q = 0; q < kRuleBatch; ++q) m4[q] = Mw[R[q].x & 0xffff];
 #pragma unroll
           for (int q = 0; q < kRuleBatch; ++q) {
             if (i0 + q >= per) break;

@@ -41,7 +41,7 @@ struct DevJob {
   const int* blk_seg;     // [nblk]
   const int* blk_ptr;     // [nblk + 1] rule range, each a multiple of 32 (lane-interleaved, padded)
   const int* blk_nrule;   // [nblk] rules of the block before padding
-  const int2* pair_rules;
+  const int2* pair_rules;   // {(j * nz + k) | target << 16, bits(w)}
 };
 
 struct DevUJob {

@@ -342,21 +342,36 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     // read as rules[i*32 + l], i = 0..per-1 (coalesced across the warp).
     // Padding rules carry the semiring zero as weight and the block's last
     // target, so they never change a cell.
+    // The device form of a rule is (j * nz + k) | target << 16: the index of
+    // its operand pair in the pair's row-major outer-product tile.
     const float zero = L.semiring == puck::SEMI_REAL ? 0.f : -INFINITY;
+    const int* pbk = L.get<int>(n + "/pair_blk", "i4", nullptr);
+    const int* ao_ = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+    const int* bo_ = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+    std::vector<int> blk_nz(nbp > 0 ? nbp - 1 : 0, 1);
+    for (int64_t k = 0; k < npk; ++k) {
+      const int cb = (pk[k] >> 8) & 255;
+      for (int b = pbk[k]; b < pbk[k + 1]; ++b) blk_nz[b] = bo_[cb + 1] - bo_[cb];
+    }
+    (void)ao_;
     std::vector<int2> rr;
     std::vector<int> dev_bp(1, 0), blk_n;
     for (int64_t b = 0; b + 1 < nbp; ++b) {
-      const int r0 = bp[b], cnt = bp[b + 1] - bp[b], per = (cnt + 31) / 32;
+      const int r0 = bp[b], cnt = bp[b + 1] - bp[b], per = (cnt + 31) / 32, nz = blk_nz[b];
       const size_t base = rr.size();
       rr.resize(base + (size_t)per * 32);
+      auto tile_form = [nz](int x) {
+        const int jj = x & 255, kk = (x >> 8) & 255;
+        return (jj * nz + kk) | (x & ~0xffff);
+      };
       for (int slot = 0; slot < per * 32; ++slot) {
         const int lane = slot % 32, i = slot / 32, logical = lane * per + i;
         int2 v;
         if (logical < cnt) {
-          v.x = pr[r0 + logical];
+          v.x = tile_form(pr[r0 + logical]);
           std::memcpy(&v.y, &pw[r0 + logical], 4);
         } else {
-          v.x = cnt ? (pr[r0 + cnt - 1] & ~0xffff) : 0;  // target kept, operands (0, 0)
+          v.x = cnt ? (pr[r0 + cnt - 1] & ~0xffff) : 0;  // target kept, operand entry 0
           std::memcpy(&v.y, &zero, 4);
         }
         rr[base + slot] = v;
