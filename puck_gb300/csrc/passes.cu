@@ -278,9 +278,20 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         float acc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q] = Sr<S>::zero();
+        if (S == SEMI_REAL) {
+          // the sum-product pass keeps one split per step
+          for (unsigned long long mm = m; mm; mm &= mm - 1) {
+            const int s = __ffsll(mm) - 1;
+            const float* A = X.aptr[c0 + s];
+            const float* B = X.bptr[c0 + s];
+            const float as = __ldg(A + ai) * X.scl[c0 + s];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (bi[q] >= 0) acc[q] = fmaf(as, __ldg(B + bi[q]), acc[q]);
+          }
+        } else
         // two live splits per step, their loads issued together; an odd last
-        // split is paired with itself (max is idempotent; the Real pass adds
-        // its second term with a zero weight), in the same order as one by one
+        // split is paired with itself (max is idempotent)
         for (unsigned long long mm = m; mm;) {
           const int s0 = __ffsll(mm) - 1;
           mm &= mm - 1;
@@ -298,14 +309,8 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
             b0v[q] = bi[q] >= 0 ? __ldg(B0 + bi[q]) : 0.f;
             b1v[q] = bi[q] >= 0 ? __ldg(B1 + bi[q]) : 0.f;
           }
-          if (S == SEMI_VITERBI) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) acc[q] = fmaxf(acc[q], fmaxf(a0v + b0v[q], a1v + b1v[q]));
-          } else {
-            const float as0 = a0v * X.scl[c0 + s0], as1 = two ? a1v * X.scl[c0 + s1] : 0.f;
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[q] = fmaf(as1, b1v[q], fmaf(as0, b0v[q], acc[q]));
-          }
+          for (int q = 0; q < 4; ++q) acc[q] = fmaxf(acc[q], fmaxf(a0v + b0v[q], a1v + b1v[q]));
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q)
@@ -317,11 +322,33 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       const int bk1 = __ldg(J.pair_blk + p + 1);
       for (int bk = __ldg(J.pair_blk + p); bk < bk1; ++bk) {
         if (gated && !gate_hit(J, __ldg(J.blk_seg + bk), ms, L.gate_merged, X.gate)) continue;
+        int cur = -1;
+        float run = Sr<S>::zero();
+        if (S == SEMI_REAL) {
+          // sum-product level: rules stored block after block, lane l reads
+          // its contiguous slice one rule per step, rule form j | k << 8
+          const int r0 = __ldg(J.blk_ptr + bk), r1 = __ldg(J.blk_ptr + bk + 1);
+          const int per = (r1 - r0 + 31) >> 5;
+          const int rs = r0 + lane * per, re = min(r1, rs + per);
+          for (int r = rs; r < re; ++r) {
+            const int2 R = __ldg(J.pair_rules + r);
+            const int jj = R.x & 255, kk = (R.x >> 8) & 255, t = (int)((unsigned)R.x >> 16);
+            const float v = Mw[jj * nz + kk] * __int_as_float(R.y);
+            if (t != cur) {
+              if (cur >= 0) flush_run<S>(P, cur, run, corner);
+              cur = t;
+              run = v;
+            } else {
+              run = Sr<S>::add(run, v);
+            }
+          }
+          if (cur >= 0) flush_run<S>(P, cur, run, corner);
+          if (lane == 0) work += (unsigned long long)(r1 - r0);
+          continue;
+        }
         // lane l runs its contiguous, target-sorted slice of the block; the
         // slices are stored interleaved, so each step's loads are coalesced
         const int r0 = __ldg(J.blk_ptr + bk), per = (__ldg(J.blk_ptr + bk + 1) - r0) >> 5;
-        int cur = -1;
-        float run = Sr<S>::zero();
         // kRuleBatch rules per step: their loads are issued before any is used
         // (the step count `per` is the same for every lane of the warp)
         for (int i0 = 0; i0 < per; i0 += kRuleBatch) {
@@ -337,7 +364,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
             if (i0 + q >= per) break;
             const int t = (int)((unsigned)R[q].x >> 16);
             const float w = __int_as_float(R[q].y);
-            const float v = S == SEMI_VITERBI ? m4[q] + w : m4[q] * w;
+            const float v = m4[q] + w;
             if (t != cur) {
               if (cur >= 0) flush_run<S>(P, cur, run, corner);
               cur = t;
@@ -448,11 +475,11 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 
 // ---------------------------------------------------------------------------
 // Inside pass over the cells of a work list (span 1: the unary layer over
-// lexicon cells).  Register budgets: six CTAs per SM in both modes (the
-// pair-factored Viterbi instance spills 32 bytes there and is still faster
-// than at five CTAs: the kernel is latency-bound).
+// lexicon cells).  Register budgets: six CTAs per SM (the pair-factored
+// Viterbi instance spills 32 bytes there and is still faster than at five
+// CTAs: the kernel is latency-bound); five for the pair-factored Real pass.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, 6)
+__global__ void __launch_bounds__(256, S == SEMI_REAL && MODE == 2 ? 5 : 6)
     k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;

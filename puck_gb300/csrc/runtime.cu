@@ -356,7 +356,19 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     (void)ao_;
     std::vector<int2> rr;
     std::vector<int> dev_bp(1, 0), blk_n;
-    for (int64_t b = 0; b + 1 < nbp; ++b) {
+    // A sum-product level keeps the archive's layout: blocks back to back,
+    // rule form j | k << 8 | target << 16.
+    const bool interleave = L.semiring == puck::SEMI_VITERBI;
+    if (!interleave) {
+      rr.resize(nbp > 0 ? bp[nbp - 1] : 0);
+      for (size_t k = 0; k < rr.size(); ++k) {
+        rr[k].x = pr[k];
+        std::memcpy(&rr[k].y, &pw[k], 4);
+      }
+      dev_bp.assign(bp, bp + nbp);
+      for (int64_t b = 0; b + 1 < nbp; ++b) blk_n.push_back(bp[b + 1] - bp[b]);
+    }
+    for (int64_t b = 0; interleave && b + 1 < nbp; ++b) {
       const int r0 = bp[b], cnt = bp[b + 1] - bp[b], per = (cnt + 31) / 32, nz = blk_nz[b];
       const size_t base = rr.size();
       rr.resize(base + (size_t)per * 32);
