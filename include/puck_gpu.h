@@ -132,6 +132,17 @@ puck_status puck_parser_stats(const puck_parser* p, puck_stats* out);
  * out[0] inside, out[1] outside, out[2] masks + scaling, out[3] decode (ms);
  * launches[0..3] the matching kernel launch counts. */
 puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[4], int64_t launches[4]);
+/* Autotuner (no reference counterpart: the reference fixes its kernel shapes
+ * when it compiles the grammar).  Parses the sample once per candidate and
+ * keeps, for the whole parser, how many waves of CTAs the cells of a span
+ * launch that does not fill the GPU are split to fill (1, 2 or 4).  chosen
+ * (levels + 1 entries, may be NULL) receives each level's gather form (0
+ * target-major, 2 pair-factored; the archive's choice) and the waves x 100.
+ * Results do not depend on the choice (Viterbi bit-identical; Real sums
+ * reorder). */
+puck_status puck_parser_autotune(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                                 int32_t* chosen);
+
 /* Binary-rule work of one level in the last call: out[0] = work units (the
  * pair-factored form: live split x child-pair elements plus applied rules;
  * the target-major form: rule x split applications), out[1] = binary partials

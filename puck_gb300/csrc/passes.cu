@@ -278,16 +278,23 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         float acc[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[q] = Sr<S>::zero();
-        if (S == SEMI_REAL) {
-          // the sum-product pass keeps one split per step
+        if (S != SEMI_VITERBI || !J.interleaved) {
+          // one split per step (the sum-product pass and the outside jobs)
           for (unsigned long long mm = m; mm; mm &= mm - 1) {
             const int s = __ffsll(mm) - 1;
             const float* A = X.aptr[c0 + s];
             const float* B = X.bptr[c0 + s];
-            const float as = __ldg(A + ai) * X.scl[c0 + s];
+            const float a = __ldg(A + ai);
+            if (S == SEMI_VITERBI) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (bi[q] >= 0) acc[q] = fmaf(as, __ldg(B + bi[q]), acc[q]);
+              for (int q = 0; q < 4; ++q)
+                if (bi[q] >= 0) acc[q] = fmaxf(acc[q], a + __ldg(B + bi[q]));
+            } else {
+              const float as = a * X.scl[c0 + s];
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                if (bi[q] >= 0) acc[q] = fmaf(as, __ldg(B + bi[q]), acc[q]);
+            }
           }
         } else
         // two live splits per step, their loads issued together; an odd last
@@ -324,16 +331,18 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         if (gated && !gate_hit(J, __ldg(J.blk_seg + bk), ms, L.gate_merged, X.gate)) continue;
         int cur = -1;
         float run = Sr<S>::zero();
-        if (S == SEMI_REAL) {
-          // sum-product level: rules stored block after block, lane l reads
-          // its contiguous slice one rule per step, rule form j | k << 8
+        if (!J.interleaved) {
+          // rules stored block after block (sum-product levels and outside
+          // jobs): lane l reads its contiguous slice one rule per step, rule
+          // form j | k << 8
           const int r0 = __ldg(J.blk_ptr + bk), r1 = __ldg(J.blk_ptr + bk + 1);
           const int per = (r1 - r0 + 31) >> 5;
           const int rs = r0 + lane * per, re = min(r1, rs + per);
           for (int r = rs; r < re; ++r) {
             const int2 R = __ldg(J.pair_rules + r);
             const int jj = R.x & 255, kk = (R.x >> 8) & 255, t = (int)((unsigned)R.x >> 16);
-            const float v = Mw[jj * nz + kk] * __int_as_float(R.y);
+            const float w = __int_as_float(R.y);
+            const float v = S == SEMI_VITERBI ? Mw[jj * nz + kk] + w : Mw[jj * nz + kk] * w;
             if (t != cur) {
               if (cur >= 0) flush_run<S>(P, cur, run, corner);
               cur = t;

@@ -35,6 +35,7 @@ struct DevJob {
   // with j, k the operands' positions among their coarse symbol's members.
   int npair;
   int a_is_t, b_is_t;
+  int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs)
   const int* pair_key;    // [npair] ca | cb << 8
   const int* pair_gate;   // [npair * mask_size] OR of the pair's segment bits
   const int* pair_blk;    // [npair + 1] block range
@@ -162,12 +163,13 @@ cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWo
 size_t pass_smem_bytes(const DevLevel& L, int chunk);
 
 // CTAs per cell of a span launch.  A cell's rule work grows with its split
-// count (span - 1).  part_target(total, sms) is the work one part should get:
-// the launch's total split count spread over two waves of CTAs (five per SM),
+// count (span - 1).  part_target(total, sms, waves) is the work one part
+// should get: the launch's total split count spread over `waves` waves of
+// CTAs (five per SM; two waves unless the parser was autotuned),
 // and at least four splits; cell_ways gives a cell enough parts for that, at
 // most 16.  A launch that already fills the GPU keeps one CTA per cell.
-inline double part_target(double total_splits, int sms) {
-  const double t = total_splits / (2.0 * sms * 5);
+inline double part_target(double total_splits, int sms, double waves = 2.0) {
+  const double t = total_splits / (waves * sms * 5);
   return t < 4.0 ? 4.0 : t;
 }
 inline int cell_ways(int span, double target) {

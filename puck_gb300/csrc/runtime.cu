@@ -356,9 +356,11 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     (void)ao_;
     std::vector<int2> rr;
     std::vector<int> dev_bp(1, 0), blk_n;
-    // A sum-product level keeps the archive's layout: blocks back to back,
-    // rule form j | k << 8 | target << 16.
-    const bool interleave = L.semiring == puck::SEMI_VITERBI;
+    // Outside jobs and sum-product levels keep the archive's layout: blocks
+    // back to back, rule form j | k << 8 | target << 16.  (The batched,
+    // interleaved form faulted the GPU in those kernels; the cause is not
+    // known, so they run the earlier, verified form.)
+    const bool interleave = L.semiring == puck::SEMI_VITERBI && j < 4;  // Viterbi inside jobs
     if (!interleave) {
       rr.resize(nbp > 0 ? bp[nbp - 1] : 0);
       for (size_t k = 0; k < rr.size(); ++k) {
@@ -393,6 +395,7 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     }
     if (rr.size() > (size_t)INT32_MAX) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule table too large in " + n};
     J.npair = (int)npk;
+    J.interleaved = interleave ? 1 : 0;
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
@@ -479,6 +482,11 @@ struct puck_parser {
   // span sequences, updated in place while a new batch keeps their shape
   std::vector<std::array<cudaGraphExec_t, 2>> graphs;
   int64_t graph_updates = 0, graph_instantiations = 0;
+  // autotuned policy: per level the gather form (-1: the archive's choice,
+  // 0 target-major, 2 pair-factored), and the waves of CTAs that long cells
+  // are split to fill
+  std::vector<int> tuned_mode;
+  double waves = 2.0;
 };
 
 namespace {
@@ -597,7 +605,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     int k = 0;
     long long cells = 0;
     while (k < ns && len[order[k]] >= L) cells += len[order[k++]] - L + 1;
-    const int G = puck::cell_ways(L, puck::part_target((double)cells * (L - 1), P->sms));
+    const int G = puck::cell_ways(L, puck::part_target((double)cells * (L - 1), P->sms, P->waves));
     ways[L] = G;
     if (G > 1) part_units = std::max(part_units, cells * G);
     span_list[L] = add_list(k, [&](int j) { return order[j]; }, [&](int j) { return (len[order[j]] - L + 1) * G; });
@@ -662,7 +670,8 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   rec(P->ev_batch[0]);
   puck::DevMask M{nullptr, 0, nullptr, nullptr};
   for (int l = 0; l < nl; ++l) {
-    const puck::DevLevel& D = P->levels[l]->d;
+    puck::DevLevel D = P->levels[l]->d;
+    if (P->tuned_mode[l] >= 0) D.mode = P->tuned_mode[l];
     const HostLevel& HL = P->g->levels[l];
     LevelBufs& lb = P->bufs[l];
     const bool last = l == nl - 1;
@@ -977,6 +986,7 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
     P->pass_launches.assign(nl, std::array<int64_t, 4>{0, 0, 0, 0});
     P->level_work.assign(nl, std::array<int64_t, 2>{0, 0});
     P->graphs.assign(nl, std::array<cudaGraphExec_t, 2>{nullptr, nullptr});
+    P->tuned_mode.assign(nl, -1);
     for (int l = 0; l < nl; ++l) {
       P->levels.emplace_back(new LevelDev());
       build_level(*P->levels.back(), g->levels[l], l < nl - 1 && nl != 1);
@@ -1077,6 +1087,47 @@ puck_status puck_debug_copy(puck_parser* P, int32_t level, int32_t which, void* 
 puck_status puck_parser_stats(const puck_parser* p, puck_stats* out) {
   if (!p || !out) return PUCK_ERR_INVALID_ARG;
   *out = p->stats;
+  return PUCK_OK;
+}
+
+puck_status puck_parser_autotune(puck_parser* P, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                                 int32_t* chosen) {
+  if (!P || nsent <= 0 || !word_ids || !offsets) {
+    set_error("puck_parser_autotune: needs a non-empty sample");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  const int nl = (int)P->levels.size();
+  std::vector<int32_t> st(nsent, 0);
+  std::vector<puck_tree_node> nodes;
+  int64_t total_nodes = 0;
+  for (int i = 0; i < nsent; ++i) total_nodes += std::max<int64_t>(2 * (offsets[i + 1] - offsets[i]) - 1, 0);
+  nodes.resize(std::max<int64_t>(total_nodes, 1));
+  // one parse of the sample; the device time of `level`'s passes, or of the
+  // whole parse with level < 0
+  auto run = [&](int level) -> double {
+    const puck_status r = run_call(P, MODE_PARSE, word_ids, offsets, nsent, nodes.data(), nullptr, st.data());
+    if (r != PUCK_OK) return -1.0;
+    if (level < 0) return P->stats.ms_device;
+    return P->pass_ms[level][0] + P->pass_ms[level][1];
+  };
+  if (run(-1) < 0) return PUCK_ERR_CUDA;  // warm-up
+  // the gather form stays the archive's choice per level (target-major or
+  // pair-factored); the tuned knob is how many waves of CTAs long cells are
+  // split to fill
+  for (int l = 0; l < nl; ++l) P->tuned_mode[l] = P->levels[l]->d.mode;
+  // waves of CTAs that split long cells
+  double best = -1.0, best_w = 2.0;
+  for (double w : {1.0, 2.0, 4.0}) {
+    P->waves = w;
+    const double t = run(-1);
+    if (t < 0) return PUCK_ERR_CUDA;
+    if (best < 0 || t < best) { best = t; best_w = w; }
+  }
+  P->waves = best_w;
+  if (chosen) {
+    for (int l = 0; l < nl; ++l) chosen[l] = P->tuned_mode[l];
+    chosen[nl] = (int32_t)(best_w * 100);
+  }
   return PUCK_OK;
 }
 

@@ -315,6 +315,15 @@ class CLParser:
         _lib.check(self._L.puck_parser_pass_ms(self._p, level, ms, n))
         return list(ms), list(n)
 
+    def autotune(self, words: np.ndarray, offsets: np.ndarray) -> dict:
+        """Runs the library's autotuner on a sample (word ids + offsets) and
+        returns the chosen gather form per level and the split waves."""
+        nl = len(self.data)
+        out = np.zeros(nl + 1, np.int32)
+        _lib.check(self._L.puck_parser_autotune(self._p, _ptr(words), _ptr(offsets), len(offsets) - 1, _ptr(out)))
+        names = {0: "target-major", 2: "pair-factored"}
+        return {"levels": [names.get(int(m), str(int(m))) for m in out[:nl]], "waves": int(out[nl]) / 100.0}
+
     def level_work(self, level: int):
         """(binary work units, +0.0 partials) of one level in the last call."""
         out = (ctypes.c_int64 * 2)()

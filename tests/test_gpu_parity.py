@@ -99,6 +99,19 @@ def test_wide_grammar_split_cells_bit_exact():
     assert np.array_equal(nodes, r.trees())
 
 
+def test_wide_grammar_fine_outside_bit_exact():
+    """insideOutside on a cascade: the fine level's pair-factored outside pass
+    (its own rule layout) against the oracle, with split cells."""
+    levels = split_levels("viterbi", "wide")
+    sents = split_sentences(24, seed=33, n_words=400, mean=24, hi=40)
+    P = gpu(levels, "split_wide")
+    words, offsets, _ = pack_sentences(sents)
+    P.inside_outside_ids(words, offsets)
+    r = oracle.run(levels, sents, mode="inside_outside")
+    assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
+    assert np.array_equal(bits(P.debug_copy(1, "outside")), bits(r.chart(1, "outside")))
+
+
 def test_wide_grammar_real_split_cells_vs_fp64():
     levels = split_levels("real", "wide")
     sents = split_sentences(24, seed=32, n_words=400, mean=24, hi=40)
@@ -137,6 +150,22 @@ def test_graph_capture_gives_identical_results():
     n2, _ = G.parse_ids(w2, o2)
     r2, _ = gpu(levels, "split_small").parse_ids(w2, o2)
     assert np.array_equal(n2, r2)
+
+
+def test_autotune_keeps_results():
+    """The autotuner may switch a level's gather form and the split waves;
+    Viterbi results stay bit-identical."""
+    levels = split_levels("viterbi", "medium")
+    sents = split_sentences(48, seed=43)
+    words, offsets, _ = pack_sentences(sents)
+    P = gpu(levels, "split_medium")
+    ref, _ = P.parse_ids(words, offsets)
+    choice = P.autotune(words, offsets)
+    assert len(choice["levels"]) == 2 and choice["waves"] in (1.0, 2.0, 4.0)
+    nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all() and np.array_equal(nodes, ref)
+    r = oracle.run(levels, sents, mode="parse")
+    assert np.array_equal(nodes, r.trees())
 
 
 def test_batching_does_not_change_results():
