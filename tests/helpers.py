@@ -28,7 +28,10 @@ def tiny_pcfg_levels(semiring="viterbi"):
 @functools.lru_cache(maxsize=None)
 def split_levels(fine_semiring="viterbi", size="medium"):
     """Coarse (Viterbi) + fine split grammar cascade."""
-    if size == "wide":
+    if size == "c1":
+        # the bench grammar: 98 coarse / 1,091 fine symbols, 1.5M binaries
+        c, f = synth.split_grammar(seed=1)
+    elif size == "wide":
         # many coarse pairs per job (hundreds of live pairs per cell), small splits
         c, f = synth.split_grammar(seed=6, n_coarse_nt=30, n_coarse_pt=20, max_split=4, mean_split=3.0,
                                    n_coarse_rules=1500, target_fine_rules=40000, n_coarse_unaries=40, n_words=400)

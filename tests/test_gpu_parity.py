@@ -99,6 +99,20 @@ def test_wide_grammar_split_cells_bit_exact():
     assert np.array_equal(nodes, r.trees())
 
 
+def test_bench_grammar_bit_exact():
+    """The 1,091-symbol, 1.5M-rule bench grammar on 40 sentences up to 40
+    words: split long cells, hundreds of live pairs, the batched inside form."""
+    levels = split_levels("viterbi", "c1")
+    sents = split_sentences(40, seed=2, n_words=40000, mean=23, hi=40)
+    P = gpu(levels, "split_c1")
+    words, offsets, _ = pack_sentences(sents)
+    nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all()
+    r = oracle.run(levels, sents, mode="parse")
+    assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
+    assert np.array_equal(nodes, r.trees())
+
+
 def test_wide_grammar_fine_outside_bit_exact():
     """insideOutside on a cascade: the fine level's pair-factored outside pass
     (its own rule layout) against the oracle, with split cells."""
