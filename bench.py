@@ -551,6 +551,50 @@ def run_long(args):
     os.unlink(path)
 
 
+def run_small(args):
+    """The plain method on the small PCFG (64 nonterminals, 32 preterminals,
+    20,000 binaries, 512 sentences of 5-20 words): FP32 inside and outside
+    plus the Viterbi tree, no pruning -- the configuration the reference's
+    own CPU path runs on."""
+    import numpy as np
+    import torch
+    from puck_gb300 import grammar, grz, synth
+    from puck_gb300.parser import CLParser, pack_sentences
+    torch.cuda.set_device(0)
+    g = synth.small_pcfg(0)
+    levels = [grammar.compile_level(g, "viterbi")]
+    path = os.path.join(tempfile.gettempdir(), f"puck_bench_small_{os.getpid()}.grz")
+    grz.write_sequence(path, levels)
+    sents = synth.uniform_sentences(args.seed, 512, 5, 20, len(g.words))
+    words, offsets, _ = pack_sentences(sents)
+    P = CLParser(path, max_alloc_size=8 << 30, profile=True, max_length=20)
+    for _ in range(args.warmup):
+        P.inside_outside_ids(words, offsets)
+        P.parse_ids(words, offsets)
+    io_ms, parse_ms = [], []
+    for _ in range(args.steps):
+        P.inside_outside_ids(words, offsets)
+        io_ms.append(P.stats()["ms_device"])
+        P.parse_ids(words, offsets)
+        parse_ms.append(P.stats()["ms_device"])
+    out = {"metric": "sentences/sec, small PCFG (64 NT + 32 PT, 20,000 binaries), len 5-20, no pruning",
+           "unit": "sentences/s", "n_gpus": 1, "dtype": "f32", "data": "synthetic",
+           "inside_outside": round(512 * len(io_ms) / (sum(io_ms) / 1e3), 1),
+           "viterbi_parse": round(512 * len(parse_ms) / (sum(parse_ms) / 1e3), 1),
+           "config": {"workload": "512 sentences uniform 5-20 words, Zipf(1.1) word ids"}}
+    if args.cpu_sample > 0:
+        import oracle
+        t0 = time.perf_counter()
+        r = oracle.run(levels, sents[:args.cpu_sample], mode="parse")
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(min(args.cpu_sample, 512) / dt, 2), "unit": "sentences/s",
+                               "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"first {min(args.cpu_sample, 512)} sentences, Viterbi parse"}
+    print(json.dumps(out), flush=True)
+    P.release()
+    os.unlink(path)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -565,9 +609,10 @@ def main():
     ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x], default="1000,2000,3000")
     ap.add_argument("--serve-sentences", type=int, default=6000)
     ap.add_argument("--serve-mem-gb", type=int, default=32)
-    ap.add_argument("--config", default="viterbi", choices=["viterbi", "mbr", "long"],
+    ap.add_argument("--config", default="viterbi", choices=["viterbi", "mbr", "long", "small"],
                     help="viterbi: the headline batched/served Viterbi cascade (default); mbr: sum-product "
-                         "MBR throughput and errors against FP64; long: long sentences on a ~2k-symbol grammar")
+                         "MBR throughput and errors against FP64; long: long sentences on a ~2k-symbol grammar; "
+                         "small: the plain method on the small PCFG")
     ap.add_argument("--fp64-subset", type=int, default=500)
     ap.add_argument("--tune-sample", type=int, default=2000, help="sentences the autotuner parses (0: no tuning)")
     ap.add_argument("--long-sentences", type=int, default=1000)
@@ -578,6 +623,8 @@ def main():
         run_mbr(args)
     elif args.config == "long":
         run_long(args)
+    elif args.config == "small":
+        run_small(args)
     else:
         run_ours(args)
 
