@@ -216,7 +216,9 @@ puck_status puck_server_take(puck_server* s, int64_t id, puck_tree_node* nodes, 
                              int32_t* sent_status, int64_t* latency_ns);
 puck_status puck_server_get_stats(const puck_server* s, puck_server_stats* out);
 /* With opts.profile: CUDA-event ms of each step kind of one level summed over
- * ticks, out[0..4] = lexicon, inside, outside, masks (+ scaling), decode. */
+ * ticks, out[0..4] = lexicon, inside, outside, masks (+ scaling), decode.
+ * With a cascade the coarse levels run as per-admission batches; their whole
+ * time is reported as level 0's inside entry. */
 puck_status puck_server_pass_ms(const puck_server* s, int32_t level, double out[5]);
 
 /* Last error message of the calling thread; returns the full length. */

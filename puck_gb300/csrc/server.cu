@@ -11,6 +11,10 @@
 //    fit, FIFO order).  The arena holds every level's charts, liveness bits,
 //    pruning masks and scales for the admitted sentences; they stay resident
 //    until the sentence's tree is decoded.
+//  * coarse groups: with a cascade, the sentences admitted in one tick run
+//    their coarse levels as one batch on a coarse stream (every span back
+//    to back), overlapping the ticks; they join the ticks at the last level
+//    once that batch is done.
 //  * ticks: every tick advances each resident sentence through its next pass
 //    steps (lexicon, inside span k, outside span k, masks, decode).  One
 //    kernel launch per step kind and level covers every sentence at that step,
@@ -141,7 +145,9 @@ struct Request {
   std::vector<puck_tree_node> nodes;
 };
 
-enum Stage { ST_LEX = 0, ST_IN = 1, ST_OUT = 2, ST_MASK = 3, ST_DEC = 4 };
+enum Stage { ST_LEX = 0, ST_IN = 1, ST_OUT = 2, ST_MASK = 3, ST_DEC = 4, ST_WAIT = 5 };
+
+constexpr int kGroups = 8;  // coarse groups in flight
 
 // A resident sentence and its pass cursor (owned by the loop thread).
 struct Resident {
@@ -150,6 +156,19 @@ struct Resident {
   long long cell_off;
   int level, stage, span;
   int upd;  // index of this tick's admission record, -1 after the admitting tick
+  int grp;  // coarse group while stage == ST_WAIT
+};
+
+// The coarse levels of the sentences admitted in one tick run as one batch
+// on the coarse stream: lexicon, every inside span, every outside span and
+// the masks, back to back.  They then join the ticks at the last level.
+struct CoarseGroup {
+  bool busy = false;
+  int waiting = 0;                 // residents still in ST_WAIT
+  cudaEvent_t begin = nullptr, done = nullptr;
+  char* host = nullptr;
+  size_t host_cap = 0;
+  DevBuf dev, parts;
 };
 
 struct Finishing {
@@ -213,6 +232,9 @@ struct puck_server {
   CellArena arena;
   std::vector<int> free_slots;
   TickBuf tb[2];
+  CoarseGroup groups[kGroups];
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t ev_slots[2] = {nullptr, nullptr};  // per tick buffer: after its slot updates
   std::vector<Resident> resident;  // loop thread only
   std::vector<StepList> lists;     // loop thread only
 
@@ -347,6 +369,118 @@ void harvest(puck_server* S, int p) {
   S->cv_done.notify_all();
 }
 
+// Launches the coarse levels of one group (the sentences admitted in one
+// tick) as a batch on the coarse stream, once tick buffer p's slot updates
+// have run: per level the lexicon, inside spans 1..n, outside spans n..1 and
+// the masks (and scales for a Real next level), each launch covering every
+// sentence of the group with cells of that span.
+void launch_group(puck_server* S, int gi, const std::vector<std::pair<int, int>>& members, int p) {
+  CoarseGroup& Gp = S->groups[gi];
+  cudaStream_t cs = S->cstream;
+  const int ns = (int)members.size();
+  std::vector<int> order(ns);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return members[a].second > members[b].second; });
+  const int maxn = members[order[0]].second;
+  std::vector<int> wl;
+  struct ListAt {
+    size_t sent, pref;
+    int nent;
+    long long nunits;
+    int span, ways;
+  };
+  auto add_list = [&](int nent, int span, int ways, auto units) {
+    ListAt at{wl.size(), 0, nent, 0, span, ways};
+    for (int k = 0; k < nent; ++k) wl.push_back(members[order[k]].first);
+    at.pref = wl.size();
+    long long acc = 0;
+    wl.push_back(0);
+    for (int k = 0; k < nent; ++k) {
+      acc += units(members[order[k]].second) * ways;
+      wl.push_back((int)acc);
+    }
+    at.nunits = acc;
+    return at;
+  };
+  std::vector<ListAt> spans(maxn + 1);
+  long long part_units = 0;
+  for (int L = 1; L <= maxn; ++L) {
+    int k = 0;
+    long long cells = 0;
+    while (k < ns && members[order[k]].second >= L) cells += members[order[k++]].second - L + 1;
+    const int G = puck::cell_ways(L, puck::part_target((double)cells * (L - 1), S->sms));
+    if (G > 1) part_units = std::max(part_units, cells * G);
+    spans[L] = add_list(k, L, G, [L](int n) { return (long long)(n - L + 1); });
+  }
+  const ListAt toks = add_list(ns, 1, 1, [](int n) { return (long long)n; });
+  const ListAt cells = add_list(ns, 0, 1, [](int n) { return 2 * tri(n); });
+  const size_t bytes = wl.size() * sizeof(int);
+  ensure_host(Gp.host, Gp.host_cap, bytes);
+  std::memcpy(Gp.host, wl.data(), bytes);
+  Gp.dev.ensure(std::max<size_t>(bytes, 16));
+  if (part_units > 0) Gp.parts.ensure(part_units * S->max_cs * sizeof(float));
+  CUDA_TRY(cudaStreamWaitEvent(cs, S->ev_slots[p], 0));
+  CUDA_TRY(cudaEventRecord(Gp.begin, cs));
+  CUDA_TRY(cudaMemcpyAsync(Gp.dev.p, Gp.host, bytes, cudaMemcpyHostToDevice, cs));
+  const int* wdev = Gp.dev.as<int>();
+  auto work = [&](const ListAt& a) {
+    puck::DevWork W{};
+    W.nent = a.nent;
+    W.nunits = a.nunits;
+    W.sent = wdev + a.sent;
+    W.span = nullptr;
+    W.span_all = a.span;
+    W.pref = wdev + a.pref;
+    W.ways = nullptr;
+    W.ways_all = a.ways;
+    W.part_rows = Gp.parts.as<float>();
+    W.cell_cnt = S->d_cell_cnt.as<int>();
+    W.one_word_batch = 0;
+    return W;
+  };
+  puck::DevBatch B{};
+  B.nsent = S->slots;
+  B.len = S->d_len.as<int>();
+  B.cell_off = S->d_cell_off.as<long long>();
+  B.word_off = S->d_cell_off.as<long long>();
+  B.words = S->d_words.as<int>();
+  B.node_off = S->d_node_off.as<long long>();
+  const puck::Counters C{S->d_counters.as<unsigned long long>(), S->d_counters.as<unsigned long long>() + 1,
+                         S->d_status.as<int>()};
+  const int maxlen = S->opt.max_length;
+  int64_t launches = 0;
+  puck::DevMask M{nullptr, 0, nullptr, nullptr};
+  for (int l = 0; l + 1 < S->nl; ++l) {
+    const puck::DevLevel& D = S->levels[l]->d;
+    LevelArena& A = S->la[l];
+    float* inside = A.inside.as<float>();
+    float* outside = A.outside.as<float>();
+    const puck::DevLive V{A.live_in.as<int>(), A.live_out.as<int>()};
+    puck::DevMask MM = M;
+    if (D.semiring != puck::SEMI_REAL) { MM.iscale = nullptr; MM.oscale = nullptr; }
+    CUDA_TRY(puck::launch_lexicon(D, B, work(toks), MM, inside, A.part.as<double>(), V, C, cs));
+    for (int L = 1; L <= maxn; ++L) CUDA_TRY(puck::launch_inside_span(D, B, work(spans[L]), MM, maxlen, inside, V, C, cs));
+    for (int L = maxn; L >= 1; --L)
+      CUDA_TRY(puck::launch_outside_span(D, B, work(spans[L]), MM, maxlen, inside, outside, V, C, cs));
+    const puck::DevWork Wc = work(cells);
+    CUDA_TRY(puck::launch_masks(D, B, Wc, inside, outside, S->opt.prune_threshold, A.masks.as<int>(), cs));
+    launches += 2 + 2 * maxn;
+    if (A.next_real) {
+      CUDA_TRY(puck::launch_scaling(D.cell_size, B, Wc, inside, A.iscale.as<float>(), cs));
+      CUDA_TRY(puck::launch_scaling(D.cell_size, B, Wc, outside, A.oscale.as<float>(), cs));
+      launches += 2;
+    }
+    M.bits = A.masks.as<int>();
+    M.mask_size = D.mask_size;
+    M.iscale = A.next_real ? A.iscale.as<float>() : nullptr;
+    M.oscale = A.next_real ? A.oscale.as<float>() : nullptr;
+  }
+  CUDA_TRY(cudaEventRecord(Gp.done, cs));
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->stats.kernel_launches += launches;
+  S->stats.h2d_bytes += (int64_t)bytes;
+}
+
 // Builds, uploads and launches one tick into buffer p.  Returns false when
 // nothing was resident.
 bool run_tick(puck_server* S, int p) {
@@ -354,16 +488,27 @@ bool run_tick(puck_server* S, int p) {
   T.launches = T.h2d = T.d2h = 0;
   std::vector<SlotUpdate> upd;
   std::vector<int> staged_words;
+  // with a cascade, this tick's admissions form one coarse group
+  const bool grouped = S->nl >= 2;
+  int gi = -1;
+  for (int k = 0; grouped && k < kGroups && gi < 0; ++k)
+    if (!S->groups[k].busy) gi = k;
+  std::vector<std::pair<int, int>> members;
   {
     std::lock_guard<std::mutex> lk(S->mu);
-    while (!S->pending.empty() && !S->free_slots.empty()) {
+    while ((!grouped || gi >= 0) && !S->pending.empty() && !S->free_slots.empty()) {
       const int64_t id = S->pending.front();
       Request& q = S->reqs[id];
       const long long off = S->arena.alloc(2 * tri(q.n));
       if (off < 0) break;
       const int slot = S->free_slots.back();
       S->free_slots.pop_back();
-      S->resident.push_back(Resident{id, slot, q.n, off, 0, ST_LEX, 0, (int)upd.size()});
+      if (grouped) {
+        S->resident.push_back(Resident{id, slot, q.n, off, S->nl - 1, ST_WAIT, 0, (int)upd.size(), gi});
+        members.emplace_back(slot, q.n);
+      } else {
+        S->resident.push_back(Resident{id, slot, q.n, off, 0, ST_LEX, 0, (int)upd.size(), -1});
+      }
       upd.push_back(SlotUpdate{off, 0, 6 * off, slot, q.n, (int)staged_words.size(), 1});
       staged_words.insert(staged_words.end(), q.words.begin(), q.words.end());
       std::vector<int>().swap(q.words);
@@ -372,6 +517,10 @@ bool run_tick(puck_server* S, int p) {
     S->stats.resident = (int64_t)S->resident.size();
     S->stats.resident_peak = std::max(S->stats.resident_peak, S->stats.resident);
     S->stats.arena_cells_peak = S->arena.peak();
+  }
+  if (!members.empty()) {
+    S->groups[gi].busy = true;
+    S->groups[gi].waiting = (int)members.size();
   }
   if (S->resident.empty()) return false;
 
@@ -386,6 +535,26 @@ bool run_tick(puck_server* S, int p) {
   std::vector<Resident> keep;
   keep.reserve(S->resident.size());
   for (Resident r : S->resident) {
+    if (r.stage == ST_WAIT) {
+      // admitted this tick (its group is not launched yet) or its coarse
+      // batch still running: not in this tick
+      CoarseGroup& Gp = S->groups[r.grp];
+      if (r.upd >= 0 || cudaEventQuery(Gp.done) != cudaSuccess) {
+        r.upd = -1;
+        keep.push_back(r);
+        continue;
+      }
+      r.stage = ST_LEX;  // level nl - 1: the coarse levels are done
+      if (--Gp.waiting == 0) {
+        float gms = 0.f;
+        if (cudaEventElapsedTime(&gms, Gp.begin, Gp.done) == cudaSuccess) {
+          std::lock_guard<std::mutex> lk(S->mu);
+          S->stats.ms_device += gms;
+          S->pass_ms[0][1] += gms;
+        }
+        Gp.busy = false;
+      }
+    }
     int last_g = -1;
     bool done = false;
     while (true) {
@@ -412,6 +581,18 @@ bool run_tick(puck_server* S, int p) {
     if (!done) keep.push_back(r);
   }
   S->resident.swap(keep);
+  // every resident sentence is waiting for its coarse batch and nothing was
+  // admitted: wait for the oldest running batch instead of an empty tick
+  bool any = !upd.empty() || !T.finishing.empty();
+  for (const auto& L : lists) any = any || !L.sent.empty();
+  if (!any) {
+    for (CoarseGroup& Gp : S->groups)
+      if (Gp.busy) {
+        CUDA_TRY(cudaEventSynchronize(Gp.done));
+        break;
+      }
+    return false;
+  }
   // span lists longest span first (their CTAs run longest)
   for (int g = 0; g < G; ++g) {
     StepList& L = lists[g];
@@ -508,6 +689,10 @@ bool run_tick(puck_server* S, int p) {
                                                         reinterpret_cast<const int*>(dbase + at_words));
     CUDA_TRY(cudaGetLastError());
     ++T.launches;
+  }
+  if (!members.empty()) {
+    CUDA_TRY(cudaEventRecord(S->ev_slots[p], st));
+    launch_group(S, gi, members, p);
   }
 
   puck::DevBatch B{};
@@ -643,7 +828,7 @@ void loop_main(puck_server* S) {
       } else if (!inflight.empty()) {
         harvest(S, inflight.front());
         inflight.pop_front();
-      } else {
+      } else if (S->resident.empty()) {
         // nothing resident and nothing admissible: wait for a submit
         std::unique_lock<std::mutex> lk(S->mu);
         S->cv_submit.wait_for(lk, std::chrono::milliseconds(1));
@@ -690,6 +875,16 @@ void destroy_server(puck_server* S) {
   S->levels.clear();
   if (S->stream) cudaStreamDestroy(S->stream);
   if (S->dstream) cudaStreamDestroy(S->dstream);
+  if (S->cstream) cudaStreamDestroy(S->cstream);
+  for (cudaEvent_t e : S->ev_slots)
+    if (e) cudaEventDestroy(e);
+  for (CoarseGroup& Gp : S->groups) {
+    if (Gp.begin) cudaEventDestroy(Gp.begin);
+    if (Gp.done) cudaEventDestroy(Gp.done);
+    if (Gp.host) cudaFreeHost(Gp.host);
+    Gp.dev.release();
+    Gp.parts.release();
+  }
   delete S;
 }
 
@@ -727,6 +922,12 @@ puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts,
     CUDA_TRY(cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, S->opt.device));
     CUDA_TRY(cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking));
     CUDA_TRY(cudaStreamCreateWithFlags(&S->dstream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&S->cstream, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : S->ev_slots) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (CoarseGroup& Gp : S->groups) {
+      CUDA_TRY(cudaEventCreate(&Gp.begin));
+      CUDA_TRY(cudaEventCreate(&Gp.done));
+    }
     for (TickBuf& T : S->tb) {
       CUDA_TRY(cudaEventCreate(&T.ev_begin));
       CUDA_TRY(cudaEventCreate(&T.ev_end));
