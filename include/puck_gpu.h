@@ -178,7 +178,10 @@ puck_status puck_mbr_decode_static(const float* cell_decode, const float* iscale
  * resident on the device, and advances all resident sentences together, one
  * pass step per sentence per tick, each kernel of a tick covering the cells
  * of every sentence at that step (sentences at different span lengths share
- * one launch).  Options as for puck_parser_create: mem_bytes sizes the chart
+ * one launch).  With a cascade, the coarse levels of the sentences admitted
+ * in one tick run as one batch on a side stream and the sentences join the
+ * ticks at the last level; the trees are decoded on a second side stream.
+ * Options as for puck_parser_create: mem_bytes sizes the chart
  * arena, max_batch_sentences caps the resident sentences (0: 65,536),
  * max_length, decode and prune_threshold as for a parse.  submit, poll, take
  * and stats may be called from any thread.  A result does not depend on which
