@@ -346,14 +346,12 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     // its operand pair in the pair's row-major outer-product tile.
     const float zero = L.semiring == puck::SEMI_REAL ? 0.f : -INFINITY;
     const int* pbk = L.get<int>(n + "/pair_blk", "i4", nullptr);
-    const int* ao_ = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
     const int* bo_ = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
     std::vector<int> blk_nz(nbp > 0 ? nbp - 1 : 0, 1);
     for (int64_t k = 0; k < npk; ++k) {
       const int cb = (pk[k] >> 8) & 255;
       for (int b = pbk[k]; b < pbk[k + 1]; ++b) blk_nz[b] = bo_[cb + 1] - bo_[cb];
     }
-    (void)ao_;
     std::vector<int2> rr;
     std::vector<int> dev_bp(1, 0), blk_n;
     // Outside jobs and sum-product levels keep the archive's layout: blocks

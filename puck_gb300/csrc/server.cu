@@ -530,7 +530,6 @@ bool run_tick(puck_server* S, int p) {
   auto& lists = S->lists;
   lists.resize(G);
   for (auto& L : lists) L.clear();
-  std::vector<std::vector<std::pair<int, int>>> spans(G);  // (span, slot) for span-ordered lists
   long long out_nodes = 0;
   std::vector<Resident> keep;
   keep.reserve(S->resident.size());
