@@ -169,6 +169,14 @@ puck_status puck_parser_level_work(const puck_parser* p, int32_t level, int64_t 
 puck_status puck_mbr_decode_static(const float* cell_decode, const float* iscale, const float* oscale,
                                    const int32_t* lengths, int32_t nsent, puck_tree_node* nodes, void* stream);
 
+/* Tensor-core check (no reference counterpart).  On `device`, one CTA
+ * computes d[128 x n] = a[128 x k] * b[n x k]^T with tcgen05.mma from shared
+ * memory into a TMEM accumulator, the building block of the BF16 sum-product
+ * rule application.  a and b are row-major BF16 bit patterns, d row-major
+ * FP32, all host memory; k and n are multiples of 16 in [16, 256].  Returns
+ * PUCK_ERR_DEVICE_TIMEOUT if the tensor-core wait gave up. */
+puck_status puck_tc_selftest(int32_t device, int32_t k, int32_t n, const uint16_t* a, const uint16_t* b, float* d);
+
 /* --- continuous-batching server ------------------------------------------
  * Replaces the reference's batching front for parse requests,
  * BatchFunctionAnnotatorService (src/main/scala/puck/AnnotatorService.scala:

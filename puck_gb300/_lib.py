@@ -53,7 +53,8 @@ class ServerStats(ctypes.Structure):
 EXPORTS = ("puck_default_options", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
            "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
-           "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_mbr_decode_static", "puck_server_create",
+           "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_mbr_decode_static",
+           "puck_tc_selftest", "puck_server_create",
            "puck_server_destroy", "puck_server_now_ns", "puck_server_submit", "puck_server_poll",
            "puck_server_take", "puck_server_get_stats", "puck_server_pass_ms", "puck_last_error")
 
@@ -102,6 +103,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_parser_level_work.restype = I
         L.puck_parser_autotune.argtypes = [P, P, P, I, P]
         L.puck_parser_autotune.restype = I
+        L.puck_tc_selftest.argtypes = [I, I, I, P, P, P]
+        L.puck_tc_selftest.restype = I
         L.puck_server_create.restype = P
         L.puck_server_create.argtypes = [P, ctypes.POINTER(Options), ctypes.POINTER(I)]
         L.puck_server_destroy.argtypes = [P]

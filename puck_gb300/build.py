@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libpuck_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["passes.cu", "decode.cu", "runtime.cu", "mbr_static.cu", "server.cu"]
+SOURCES = ["passes.cu", "decode.cu", "runtime.cu", "mbr_static.cu", "server.cu", "tensor.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
