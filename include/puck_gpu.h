@@ -58,6 +58,9 @@ typedef struct puck_options {
   int32_t max_batch_sentences;/* cap on sentences per batch (0: no cap beyond memory) */
   float prune_threshold;      /* coarse-pass log max-marginal threshold (reference: -9, CLParser.scala:226) */
   int32_t use_graphs;         /* non-zero: capture each batch's pass sequence in a CUDA graph */
+  int32_t tensor_cores;       /* non-zero: the sum-product fine level's inside binary sums run on
+                                 tcgen05 tensor cores in BF16 with FP32 accumulation (levels whose
+                                 structure the form does not cover keep the FP32 path) */
 } puck_options;
 
 /* One node of a preorder tree (the reference's tree_t, CLViterbi.scala:378):
@@ -142,6 +145,11 @@ puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[
  * reorder). */
 puck_status puck_parser_autotune(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
                                  int32_t* chosen);
+
+/* 1 if `level` runs its inside binary sums on tensor cores (options
+ * tensor_cores and a level the form covers), 0 if not (why, may be NULL,
+ * receives the reason), -1 for a bad level. */
+int32_t puck_parser_tensor_cores(const puck_parser* p, int32_t level, char* why, size_t len);
 
 /* Binary-rule work of one level in the last call: out[0] = work units (the
  * pair-factored form: live split x child-pair elements plus applied rules;

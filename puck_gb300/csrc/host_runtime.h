@@ -73,6 +73,9 @@ struct DevBuf {
 struct LevelDev {
   std::vector<void*> allocs;
   puck::DevLevel d{};
+  puck::DevTc tc{};
+  bool tc_ok = false;     // the tensor-core tables were built
+  std::string tc_why;     // else why not
   void* upload(const void* src, size_t bytes) {
     void* p = nullptr;
     CUDA_TRY(cudaMalloc(&p, std::max<size_t>(bytes, 16)));
@@ -87,6 +90,9 @@ struct LevelDev {
 
 // Uploads a level's tables (rule CSR, pair tables, lexicon, Viterbi tables).
 void build_level(LevelDev& D, const HostLevel& L, bool merged);
+// Uploads a sum-product level's tensor-core tables (DevTc) after build_level;
+// false, with the reason, if the level's structure is not covered.
+bool build_tc(LevelDev& D, const HostLevel& L, std::string* why);
 
 }  // namespace puck_host
 

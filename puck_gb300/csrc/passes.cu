@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(256, S == SEMI_REAL && MODE == 2 ? 5 : 6)
     X.work = 0;
     X.corner = 0;
     // a pruned cell has no rule work: part 0 finishes it alone
-    X.G = X.flag0 && span >= 2 ? G : 1;
+    X.G = X.flag0 && span >= 2 && !(S == SEMI_REAL && L.tc_binary) ? G : 1;
     X.g = X.flag0 && span >= 2 ? g : 0;
     if (M.bits)
       for (int i = 0; i < ms; ++i) X.gate[i] = M.bits[pbot * ms + i];
@@ -525,7 +525,8 @@ __global__ void __launch_bounds__(256, S == SEMI_REAL && MODE == 2 ? 5 : 6)
       add_split<S>(X, inside + lc * cs, inside + rc * cs, V.in + lc * ms, V.in + rc * ms, scale_of(M.iscale, lc),
                    scale_of(M.iscale, rc), ps);
   };
-  if (span == 1) {
+  if (span == 1 || (S == SEMI_REAL && L.tc_binary && X.flag0)) {
+    // lexicon scores, or binary sums the tensor-core pass left in the bot cell
     for (int k = threadIdx.x; k < cs; k += blockDim.x) P[k] = inside[pbot * cs + k];
   } else if (X.flag0) {
     for (int job = 0; job < 4; ++job) {

@@ -57,6 +57,7 @@ struct DevLevel {
   int mode;         // 0: target-major rule scans, 2: pair-factored
   int max_npair;    // largest pair count of any job (shared-memory list size)
   int max_mtile;    // largest ny * nz of any pair (per-warp outer-product tile)
+  int tc_binary;    // sum-product inside pass: binary sums already in the bot cells (tensor-core form)
   const int* nt_mem_off;  // [n_coarse + 1] coarse -> nonterminal members
   const int* nt_mem;
   const int* t_mem_off;   // [n_coarse + 1] coarse -> terminal members
@@ -72,6 +73,33 @@ struct DevLevel {
   const int* v_left;
   const int* v_right;
   const float* v_score;
+};
+
+// Tensor-core form of a sum-product level's inside binary pass.  The binary
+// sums of a tile of 128 cells accumulate in TMEM, one FP32 column per target:
+// targets are grouped by coarse parent into slots of slot_w columns, and the
+// slots are split into nparts parts of at most ncols columns (one CTA per
+// tile and part).  For every rule block of a coarse pair the block's weights
+// form a BF16 B operand (slot_w rows = the parent's members, kpad columns =
+// the pair's outer-product tile padded to 16), stored in the tcgen05 K-major
+// core-matrix layout; the pair's outer products over the cell's live splits
+// form the A operand (128 cells x kpad).  Gating by the cell mask is applied
+// per target when the accumulator is read out: every target keeps the same
+// segment bits in every job and block, which the builder checks.
+struct DevTc {
+  int nparts, slot_w, ncols;  // ncols: TMEM columns allocated (a power of two, <= 512)
+  int max_kpad, bcap;         // largest kpad; bytes of one B staging buffer
+  const int* part_off;        // [nparts + 1] into tpair
+  const int4* tpair;          // {job | pair << 2, kpad, blk0, blk1}: a pair's blocks in one part
+  const int* tpair_gate;      // [ntpair * mask_size] OR of those blocks' segment bits
+  const int* tblk;            // [nblk] TMEM slot of a block; its B operand follows the previous one's
+  const long long* tpair_b;   // [ntpair] byte offset of the entry's first B operand in bmat
+  const unsigned char* bmat;  // B operands, BF16
+  const int* col_tgt;         // [nparts * ncols] target of a column, -1 for none
+  const int* tgt_gate;        // [n_nt * mask_size] segment bits of each binary target
+  const int* uncovered;       // row positions no column covers (written as zero)
+  int n_uncovered;
+  int* err;                   // set when a tensor-core wait gave up; later CTAs then skip their tiles
 };
 
 // Sentences of a batch (or of a server's resident set).  Each sentence's
@@ -161,6 +189,17 @@ cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWo
                                const float* inside, const double* part_scale, float* log_z, cudaStream_t st);
 
 size_t pass_smem_bytes(const DevLevel& L, int chunk);
+
+// Tensor-core inside pass: the binary sums of the cells of one span.  cells
+// holds (sentence, begin) pairs; 128 cells per tile, one CTA per tile and
+// TMEM part.  The cells are finished by launch_inside_span with
+// L.tc_binary set.
+constexpr int kTcRows = 128;
+constexpr int kTcThreads = 512;
+size_t tc_smem_bytes(const DevTc& T);
+size_t tc_static_smem_bytes();
+cudaError_t launch_inside_tc(const DevLevel& L, const DevTc& T, const DevBatch& B, int span, const int* cells,
+                             int ncells, const DevMask& M, float* inside, DevLive V, Counters C, cudaStream_t st);
 
 // CTAs per cell of a span launch.  A cell's rule work grows with its split
 // count (span - 1).  part_target(total, sms, waves) is the work one part

@@ -447,6 +447,208 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
 
 namespace {
 
+uint16_t bf16_bits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;  // NaN
+  return (uint16_t)((u + 0x7fffu + ((u >> 16) & 1u)) >> 16);  // round to nearest even
+}
+
+int tile_offset_host(int r, int k, int kpad) { return ((r >> 3) * (kpad >> 3) + (k >> 3)) * 128 + (r & 7) * 16 + (k & 7) * 2; }
+
+}  // namespace
+
+// Tensor-core tables of a sum-product level (DevTc).  Returns false, with the
+// reason, for a level whose structure the tensor-core form does not cover.
+bool puck_host::build_tc(LevelDev& D, const HostLevel& L, std::string* why) {
+  auto no = [&](const std::string& m) {
+    if (why) *why = m;
+    return false;
+  };
+  const puck::DevLevel& d = D.d;
+  if (L.semiring != puck::SEMI_REAL || d.mode != 2) return no("not a pair-factored sum-product level");
+  if (d.gate_merged) return no("coarse level of a cascade");
+  const int ms = L.mask_size, cs = L.cell_size;
+  const int* nt_off = L.get<int>("nt_mem_off", "i4", nullptr);
+  const int* nt_mem = L.get<int>("nt_mem", "i4", nullptr);
+  const int* t_off = L.get<int>("t_mem_off", "i4", nullptr);
+  const int* ntc = L.get<int>("nt_coarse", "i4", nullptr);
+  // member index of each nonterminal within its coarse symbol
+  std::vector<int> memidx(L.n_nt, -1);
+  int maxmem = 0;
+  for (int c = 0; c < L.n_coarse; ++c) {
+    maxmem = std::max(maxmem, nt_off[c + 1] - nt_off[c]);
+    for (int i = nt_off[c]; i < nt_off[c + 1]; ++i) memidx[nt_mem[i]] = i - nt_off[c];
+  }
+  const int slot_w = (maxmem + 15) / 16 * 16;
+  if (slot_w > 32) return no("more than 32 refinements of a coarse symbol");
+  // Gating.  A target whose segment bits are the same in every block of the
+  // four inside jobs is gated when the accumulator is read out.  Rules of
+  // any other target go into entries of their own, one per segment, whose
+  // rows are zeroed for the cells the segment does not gate in.
+  std::vector<std::vector<int>> tbits(L.n_nt);
+  std::vector<char> incons(L.n_nt, 0), parent_used(L.n_coarse, 0);
+  int max_kpad = 16;
+  struct JobTabs {
+    int64_t npk = 0;
+    const int *pk, *pbk, *bp, *bs, *sb, *pr;
+    const float* pw;
+    const int *ao, *bo;
+  };
+  JobTabs jt[4];
+  for (int j = 0; j < 4; ++j) {
+    const std::string n = kJobNames[j];
+    JobTabs& J = jt[j];
+    J.pk = L.get<int>(n + "/pair_key", "i4", &J.npk);
+    J.pbk = L.get<int>(n + "/pair_blk", "i4", nullptr);
+    J.bp = L.get<int>(n + "/blk_ptr", "i4", nullptr);
+    J.bs = L.get<int>(n + "/blk_seg", "i4", nullptr);
+    J.sb = L.get<int>(n + "/seg_bits", "i4", nullptr);
+    J.pr = L.get<int>(n + "/pair_rule", "i4", nullptr);
+    J.pw = L.get<float>(n + "/pair_w", "f4", nullptr);
+    const bool at = j == 2 || j == 3, bt = j == 1 || j == 3;
+    J.ao = at ? t_off : nt_off;
+    J.bo = bt ? t_off : nt_off;
+    for (int64_t p = 0; p < J.npk; ++p) {
+      const int ca = J.pk[p] & 255, cb = (J.pk[p] >> 8) & 255;
+      const int kk = (J.ao[ca + 1] - J.ao[ca]) * (J.bo[cb + 1] - J.bo[cb]);
+      if (kk > 256) return no("a coarse pair with more than 256 child pairs");
+      max_kpad = std::max(max_kpad, (kk + 15) / 16 * 16);
+      for (int b = J.pbk[p]; b < J.pbk[p + 1]; ++b) {
+        const std::vector<int> bits(J.sb + (size_t)J.bs[b] * ms, J.sb + (size_t)(J.bs[b] + 1) * ms);
+        for (int r = J.bp[b]; r < J.bp[b + 1]; ++r) {
+          const int t = (int)((unsigned)J.pr[r] >> 16);
+          if (t < 0 || t >= L.n_nt) return no("binary target outside the nonterminals");
+          parent_used[ntc[t]] = 1;
+          if (tbits[t].empty()) tbits[t] = bits;
+          else if (tbits[t] != bits) incons[t] = 1;
+        }
+      }
+    }
+  }
+  std::vector<int> tgt_gate((size_t)L.n_nt * ms, -1);
+  for (int t = 0; t < L.n_nt; ++t)
+    if (!incons[t] && !tbits[t].empty()) std::memcpy(&tgt_gate[(size_t)t * ms], tbits[t].data(), ms * sizeof(int));
+  // slots: coarse parents in order, split evenly over parts of <= 512 columns
+  std::vector<int> parents;
+  for (int c = 0; c < L.n_coarse; ++c)
+    if (parent_used[c]) parents.push_back(c);
+  if (parents.empty()) return no("no binary rules");
+  const int per_part_max = 512 / slot_w;
+  const int nparts = ((int)parents.size() + per_part_max - 1) / per_part_max;
+  const int per_part = ((int)parents.size() + nparts - 1) / nparts;
+  int ncols = 64;  // a multiple of 64: four warps zero and read a quarter each, 16 columns at a time
+  while (ncols < per_part * slot_w) ncols <<= 1;
+  std::vector<int> part_of(L.n_coarse, -1), slot_of(L.n_coarse, -1);
+  std::vector<int> col_tgt((size_t)nparts * ncols, -1);
+  std::vector<char> covered(cs, 0);
+  for (size_t i = 0; i < parents.size(); ++i) {
+    const int c = parents[i], h = (int)i / per_part, sl = (int)i % per_part;
+    part_of[c] = h;
+    slot_of[c] = sl;
+    for (int m = 0; m < nt_off[c + 1] - nt_off[c]; ++m) {
+      col_tgt[(size_t)h * ncols + sl * slot_w + m] = nt_mem[nt_off[c] + m];
+      covered[nt_mem[nt_off[c] + m]] = 1;
+    }
+  }
+  std::vector<int> uncovered;
+  for (int k = 0; k < cs; ++k)
+    if (!covered[k]) uncovered.push_back(k);
+  // shared memory: two A tiles (128 x max_kpad BF16) and two B buffers
+  const size_t static_smem = puck::tc_static_smem_bytes() + 256;
+  const size_t abytes = 2 * (size_t)puck::kTcRows * max_kpad * 2;
+  const size_t blk_bytes = (size_t)slot_w * max_kpad * 2;
+  if (abytes + static_smem + 2 * blk_bytes > 227 * 1024) return no("outer-product tiles too large for shared memory");
+  size_t bcap = std::min<size_t>(40 * 1024, (227 * 1024 - static_smem - abytes) / 2);
+  // a CTA holding more than half of TMEM keeps its SM to itself (a second
+  // one would wait in tcgen05.alloc): shared memory for one CTA per SM
+  if (ncols > 256 && abytes + 2 * bcap + static_smem < 120 * 1024) bcap = (120 * 1024 - abytes - static_smem + 1) / 2;
+  bcap = (bcap + 127) / 128 * 128;
+  if (abytes + 2 * bcap + static_smem > 227 * 1024) return no("tensor-core buffers do not fit shared memory");
+  // Entries, per part, job and pair: the pair's freely gated rules, then one
+  // entry per segment for rules of targets with differing segments.  An
+  // entry's B operands are one tile per coarse parent (slot), split into
+  // several entries when they exceed a staging buffer.
+  std::vector<int4> tpair;
+  std::vector<int> tpair_gate, tblk, part_off(1, 0);
+  std::vector<long long> tpair_b;
+  std::vector<uint16_t> bmat;
+  for (int h = 0; h < nparts; ++h) {
+    for (int j = 0; j < 4; ++j) {
+      const JobTabs& J = jt[j];
+      for (int64_t p = 0; p < J.npk; ++p) {
+        const int ca = J.pk[p] & 255, cb = (J.pk[p] >> 8) & 255;
+        const int nz = J.bo[cb + 1] - J.bo[cb];
+        const int kpad = ((J.ao[ca + 1] - J.ao[ca]) * nz + 15) / 16 * 16;
+        const size_t bbytes = (size_t)slot_w * kpad * 2;
+        // entry key: empty = readout-gated rules, else the segment bits
+        std::map<std::vector<int>, std::map<int, std::vector<int>>> groups;  // key -> slot -> rules
+        std::map<std::vector<int>, std::vector<int>> gate_of;
+        for (int b = J.pbk[p]; b < J.pbk[p + 1]; ++b) {
+          const std::vector<int> bits(J.sb + (size_t)J.bs[b] * ms, J.sb + (size_t)(J.bs[b] + 1) * ms);
+          for (int r = J.bp[b]; r < J.bp[b + 1]; ++r) {
+            const int t = (int)((unsigned)J.pr[r] >> 16), parent = ntc[t];
+            if (part_of[parent] != h) continue;
+            const std::vector<int> key = incons[t] ? bits : std::vector<int>();
+            groups[key][slot_of[parent]].push_back(r);
+            std::vector<int>& g = gate_of[key];
+            if (g.empty()) g.assign(ms, 0);
+            for (int w = 0; w < ms; ++w) g[w] |= bits[w];
+          }
+        }
+        for (auto& kv : groups) {
+          std::vector<std::pair<int, const std::vector<int>*>> tiles;
+          for (auto& sv : kv.second) tiles.emplace_back(sv.first, &sv.second);
+          const std::vector<int>& gate = gate_of[kv.first];
+          for (size_t i0 = 0; i0 < tiles.size();) {
+            const size_t take = std::min(tiles.size() - i0, bcap / bbytes);
+            int4 e;
+            e.x = j | (int)(p << 2);
+            e.y = kpad;
+            e.z = (int)tblk.size();
+            e.w = e.z + (int)take;
+            tpair.push_back(e);
+            tpair_b.push_back((long long)bmat.size() * 2);
+            tpair_gate.insert(tpair_gate.end(), gate.begin(), gate.end());
+            for (size_t i = i0; i < i0 + take; ++i) {
+              tblk.push_back(tiles[i].first);
+              const size_t base = bmat.size();
+              bmat.resize(base + bbytes / 2, 0);
+              for (int r : *tiles[i].second) {
+                const int jj = J.pr[r] & 255, kk = (J.pr[r] >> 8) & 255, t = (int)((unsigned)J.pr[r] >> 16);
+                bmat[base + tile_offset_host(memidx[t], jj * nz + kk, kpad) / 2] = bf16_bits(J.pw[r]);
+              }
+            }
+            i0 += take;
+          }
+        }
+      }
+    }
+    part_off.push_back((int)tpair.size());
+  }
+  puck::DevTc& T = D.tc;
+  T.nparts = nparts;
+  T.slot_w = slot_w;
+  T.ncols = ncols;
+  T.max_kpad = max_kpad;
+  T.bcap = (int)bcap;
+  T.part_off = static_cast<const int*>(D.upload(part_off.data(), part_off.size() * sizeof(int)));
+  T.tpair = static_cast<const int4*>(D.upload(tpair.data(), tpair.size() * sizeof(int4)));
+  T.tpair_gate = static_cast<const int*>(D.upload(tpair_gate.data(), tpair_gate.size() * sizeof(int)));
+  T.tblk = static_cast<const int*>(D.upload(tblk.data(), tblk.size() * sizeof(int)));
+  T.tpair_b = static_cast<const long long*>(D.upload(tpair_b.data(), tpair_b.size() * sizeof(long long)));
+  T.bmat = static_cast<const unsigned char*>(D.upload(bmat.data(), bmat.size() * 2));
+  T.col_tgt = static_cast<const int*>(D.upload(col_tgt.data(), col_tgt.size() * sizeof(int)));
+  T.tgt_gate = static_cast<const int*>(D.upload(tgt_gate.data(), tgt_gate.size() * sizeof(int)));
+  T.uncovered = static_cast<const int*>(D.upload(uncovered.data(), uncovered.size() * sizeof(int)));
+  T.n_uncovered = (int)uncovered.size();
+  const int zero = 0;
+  T.err = static_cast<int*>(D.upload(&zero, sizeof(int)));
+  return true;
+}
+
+namespace {
+
 long long tri(int n) { return (long long)n * (n + 1) / 2; }
 
 enum Mode { MODE_PARSE = 0, MODE_PARTITIONS = 1, MODE_INSIDE_OUTSIDE = 2 };
@@ -608,6 +810,26 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     if (G > 1) part_units = std::max(part_units, cells * G);
     span_list[L] = add_list(k, [&](int j) { return order[j]; }, [&](int j) { return (len[order[j]] - L + 1) * G; });
   }
+  // tensor-core inside passes: per span, the (sentence, begin) pairs of its
+  // cells in tiles, and a one-CTA-per-cell list for finishing the cells
+  const bool any_tc = std::any_of(P->levels.begin(), P->levels.end(), [](const auto& x) { return x->tc_ok; });
+  std::vector<ListAt> span_list1;
+  std::vector<std::pair<size_t, int>> tc_cells(max_len + 1, {0, 0});
+  if (any_tc) {
+    span_list1.resize(max_len + 1);
+    for (int L = 1; L <= max_len; ++L) {
+      int k = 0;
+      while (k < ns && len[order[k]] >= L) ++k;
+      span_list1[L] = add_list(k, [&](int j) { return order[j]; }, [&](int j) { return len[order[j]] - L + 1; });
+      tc_cells[L].first = wl.size();
+      for (int j = 0; j < k; ++j)
+        for (int b = 0; b + L <= len[order[j]]; ++b) {
+          wl.push_back(order[j]);
+          wl.push_back(b);
+        }
+      tc_cells[L].second = (int)((wl.size() - tc_cells[L].first) / 2);
+    }
+  }
   const ListAt tok_list = add_list(ns, [](int j) { return j; }, [&](int j) { return len[j]; });
   const ListAt cell_list = add_list(ns, [](int j) { return j; }, [&](int j) { return 2 * tri(len[j]); });
   const long long num_cells = cell_off[ns];
@@ -670,6 +892,9 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   for (int l = 0; l < nl; ++l) {
     puck::DevLevel D = P->levels[l]->d;
     if (P->tuned_mode[l] >= 0) D.mode = P->tuned_mode[l];
+    const bool tc = P->levels[l]->tc_ok && D.mode == 2 && num_cells < INT32_MAX;
+    D.tc_binary = tc ? 1 : 0;
+    if (tc) CUDA_TRY(cudaMemsetAsync(P->levels[l]->tc.err, 0, sizeof(int), st));
     const HostLevel& HL = P->g->levels[l];
     LevelBufs& lb = P->bufs[l];
     const bool last = l == nl - 1;
@@ -695,7 +920,16 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
       CUDA_TRY(puck::launch_lexicon(D, B, Wtok, MM, inside, lb.part.as<double>(), V, C, st));
       ++LC[0];
       for (int span = 1; span <= max_len; ++span) {
-        CUDA_TRY(puck::launch_inside_span(D, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
+        if (tc && span >= 2) {
+          CUDA_TRY(puck::launch_inside_tc(D, P->levels[l]->tc, B, span, wdev + tc_cells[span].first,
+                                          tc_cells[span].second, MM, inside, V, C, st));
+          ++LC[0];
+          puck::DevWork W1 = work(span_list1[span], span);
+          W1.ways_all = 1;
+          CUDA_TRY(puck::launch_inside_span(D, B, W1, MM, max_len, inside, V, C, st));
+        } else {
+          CUDA_TRY(puck::launch_inside_span(D, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
+        }
         ++LC[0];
       }
     });
@@ -918,6 +1152,7 @@ void puck_default_options(puck_options* o) {
   o->max_batch_sentences = 0;
   o->prune_threshold = -9.0f;
   o->use_graphs = 0;
+  o->tensor_cores = 0;
 }
 
 puck_grammar* puck_grammar_load(const char* path, puck_status* status) {
@@ -987,7 +1222,9 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
     P->tuned_mode.assign(nl, -1);
     for (int l = 0; l < nl; ++l) {
       P->levels.emplace_back(new LevelDev());
-      build_level(*P->levels.back(), g->levels[l], l < nl - 1 && nl != 1);
+      LevelDev& LD = *P->levels.back();
+      build_level(LD, g->levels[l], l < nl - 1 && nl != 1);
+      if (P->opt.tensor_cores && l == nl - 1) LD.tc_ok = build_tc(LD, g->levels[l], &LD.tc_why);
     }
     P->bufs.resize(nl);
     size_t free_b = 0, total_b = 0;
@@ -1127,6 +1364,18 @@ puck_status puck_parser_autotune(puck_parser* P, const int32_t* word_ids, const 
     chosen[nl] = (int32_t)(best_w * 100);
   }
   return PUCK_OK;
+}
+
+int32_t puck_parser_tensor_cores(const puck_parser* p, int32_t level, char* why, size_t len) {
+  if (!p || level < 0 || level >= (int)p->levels.size()) return -1;
+  const LevelDev& L = *p->levels[level];
+  if (why && len) {
+    const std::string m = L.tc_ok ? std::string() : (p->opt.tensor_cores ? L.tc_why : "tensor cores not requested");
+    const size_t k = std::min(len - 1, m.size());
+    std::memcpy(why, m.data(), k);
+    why[k] = 0;
+  }
+  return L.tc_ok ? 1 : 0;
 }
 
 puck_status puck_parser_level_work(const puck_parser* p, int32_t level, int64_t out[2]) {

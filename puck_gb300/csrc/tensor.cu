@@ -13,12 +13,13 @@
 
 #include "../../include/puck_gpu.h"
 #include "puck_internal.h"
+#include "device_common.cuh"
 #include "tcgen05.cuh"
 
 namespace puck {
 namespace {
 
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s for any tensor-core wait
+constexpr unsigned long long kWaitNs = 500000000ull;  // 0.5 s for any tensor-core wait
 
 __device__ __forceinline__ int pow2_cols(int n) {
   int c = 32;
@@ -79,7 +80,309 @@ __global__ void __launch_bounds__(128, 1)
   if (threadIdx.x < 32) tc::tmem_dealloc(taddr, ncols);
 }
 
+// ---------------------------------------------------------------------------
+// Sum-product inside pass on tensor cores: binary sums of a tile of 128 cells
+// of one span, for the targets of one TMEM part (see DevTc).  For every coarse
+// pair with rule blocks in the part, the CUDA cores build the pair's
+// outer-product rows M_c[j*nz + k] = sum_s scale_s * A_s[Y_j] * B_s[Z_k] over
+// each cell's live splits (FP32, rounded to BF16 into the A operand; a cell
+// for which the pair is dead gets a zero row), the block weights are copied
+// into the B operand, and one elected thread issues the MMAs that add
+// A x B^T into the block's TMEM slot.  Two A/B buffers alternate, so the
+// CUDA cores fill one while the tensor core reads the other.  The
+// accumulator is read out once, gated per target by the cell mask, into the
+// bot cells; launch_inside_span (tc_binary) then finishes the cells.
+//
+// Reference: the inside binary pass (src/main/scala/puck/parser/
+// CLParser.scala:489-504) with the Real semiring's scaled products
+// (src/main/java/puck/parser/gen/SimpleGenRuleMultiply.java:213-214).
+struct TcCells {
+  long long pbot[kTcRows];
+  int sent[kTcRows], beg[kTcRows], len[kTcRows];
+  float ps[kTcRows];
+  int flag[kTcRows];                        // valid and unpruned
+  int gate[kTcRows][kMaxMask];
+  unsigned allow[kTcRows][kMaxLen / 32];    // NN: split b + 1 + i has both operand cells unpruned
+  unsigned char allow1[kTcRows][4];         // NT, TN, TT
+  uint32_t taddr;
+  int err;
+  uint64_t bar[2], bar_fin;
+};
+
+constexpr int kTcRounds = 4;  // outer-product tasks per lane (ny * ceil(nz / 4) <= 128)
+
+__device__ __forceinline__ bool live_bit(const int* live, long long cell, int ms, int c) {
+  return (__ldg(live + cell * ms + (c >> 5)) >> (c & 31)) & 1;
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_inside_tc(DevLevel L, DevTc T, DevBatch B, int span, const int* cells, int ncells, DevMask M, float* inside,
+                DevLive V, Counters C) {
+  using namespace dev;
+  extern __shared__ __align__(1024) unsigned char sm_raw[];
+  __shared__ TcCells X;
+  const int cs = L.cell_size, ms = L.mask_size, h = blockIdx.y;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t abytes = (size_t)kTcRows * T.max_kpad * 2;
+  unsigned char* sA[2] = {sm_raw, sm_raw + abytes};
+  unsigned char* sB[2] = {sm_raw + 2 * abytes, sm_raw + 2 * abytes + T.bcap};
+  // --- the tile's cells ----------------------------------------------------
+  if (tid < kTcRows) {
+    const int c = blockIdx.x * kTcRows + tid;
+    const bool valid = c < ncells;
+    const int s = valid ? cells[2 * c] : 0, b = valid ? cells[2 * c + 1] : 0;
+    const int n = valid ? B.len[s] : 0, e = b + span;
+    const long long off = valid ? B.cell_off[s] : 0, toff = off + tri(n);
+    const long long pbot = valid ? off + chart_index(b, e, n) : 0;
+    const bool f = valid && mask_any(M, pbot);
+    X.pbot[tid] = pbot;
+    X.sent[tid] = s;
+    X.beg[tid] = b;
+    X.len[tid] = n;
+    X.flag[tid] = f;
+    X.ps[tid] = f ? scale_of(M.iscale, pbot) : 0.f;
+    for (int i = 0; i < ms; ++i) X.gate[tid][i] = f && M.bits ? M.bits[pbot * ms + i] : -1;
+    for (int w = 0; w < kMaxLen / 32; ++w) X.allow[tid][w] = 0u;
+    if (f) {
+      auto BOT = [&](int x, int y) { return off + chart_index(x, y, n); };
+      auto TOP = [&](int x, int y) { return toff + chart_index(x, y, n); };
+      for (int sp = b + 1; sp < e; ++sp)
+        if (mask_any(M, TOP(b, sp)) && mask_any(M, TOP(sp, e))) X.allow[tid][(sp - b - 1) >> 5] |= 1u << ((sp - b - 1) & 31);
+      X.allow1[tid][0] = mask_any(M, TOP(b, e - 1)) && mask_any(M, BOT(e - 1, e));
+      X.allow1[tid][1] = mask_any(M, BOT(b, b + 1)) && mask_any(M, TOP(b + 1, e));
+      X.allow1[tid][2] = span == 2 && mask_any(M, BOT(b, b + 1)) && mask_any(M, BOT(b + 1, e));
+    } else {
+      X.allow1[tid][0] = X.allow1[tid][1] = X.allow1[tid][2] = 0;
+    }
+  }
+  // a wait of an earlier CTA gave up: this launch's results are void
+  if (tid == 0) X.err = *reinterpret_cast<volatile int*>(T.err);
+  __syncthreads();
+  if (X.err) {
+    if (tid < kTcRows && X.flag[tid] && C.status) C.status[X.sent[tid]] = 5;  // PUCK_ERR_DEVICE_TIMEOUT
+    return;
+  }
+  if (warp == 0) tc::tmem_alloc(&X.taddr, T.ncols);
+  if (tid == 0) {
+    tc::mbar_init(&X.bar[0], 1);
+    tc::mbar_init(&X.bar[1], 1);
+    tc::mbar_init(&X.bar_fin, 1);
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = X.taddr;
+  // --- zero the accumulator --------------------------------------------------
+  {
+    const int q = warp & 3, chunk = warp >> 2, per = T.ncols / 4;
+    for (int c = chunk * per; c < (chunk + 1) * per; c += 16) tc::tmem_st16_zero(taddr + ((uint32_t)(q * 32) << 16) + c);
+    tc::tmem_wait_st();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  // --- the part's pairs -------------------------------------------------------
+  const uint32_t idesc = tc::idesc_bf16_f32(kTcRows, T.slot_w);
+  unsigned ncommit[2] = {0u, 0u};
+  int it = 0;
+  bool issued = false;
+  for (int e = T.part_off[h]; e < T.part_off[h + 1]; ++e) {
+    const int4 tp = __ldg(T.tpair + e);
+    const int job = tp.x & 3, p = tp.x >> 2, kpad = tp.y, nb = tp.w - tp.z;
+    if (job == IN_TT && span != 2) continue;
+    const DevJob& J = L.jobs[job];
+    const int buf = it & 1;
+    if (ncommit[buf] && !X.err && !tc::mbar_wait(&X.bar[buf], (ncommit[buf] - 1) & 1, kWaitNs)) {
+      atomicExch(&X.err, 1);
+      atomicExch(T.err, 1);
+    }
+    tc::fence_after_sync();
+    // B operands of the entry's blocks, contiguous in bmat
+    {
+      const uint4* src = reinterpret_cast<const uint4*>(T.bmat + __ldg(T.tpair_b + e));
+      uint4* dst = reinterpret_cast<uint4*>(sB[buf]);
+      const int n16 = nb * T.slot_w * kpad * 2 / 16;
+      for (int i = tid; i < n16; i += kTcThreads) dst[i] = __ldg(src + i);
+    }
+    // A operand: one row per cell
+    const int key = __ldg(J.pair_key + p);
+    const int ca = key & 255, cb = (key >> 8) & 255;
+    const int* aoff = J.a_is_t ? L.t_mem_off : L.nt_mem_off;
+    const int* amem = J.a_is_t ? L.t_mem : L.nt_mem;
+    const int* boff = J.b_is_t ? L.t_mem_off : L.nt_mem_off;
+    const int* bmem = J.b_is_t ? L.t_mem : L.nt_mem;
+    const int a0 = __ldg(aoff + ca), ny = __ldg(aoff + ca + 1) - a0;
+    const int b0 = __ldg(boff + cb), nz = __ldg(boff + cb + 1) - b0;
+    const int kk = ny * nz, nkq = (nz + 3) >> 2, ntask = ny * nkq;
+    const int* pg = T.tpair_gate + (size_t)e * ms;
+    int local_any = 0;
+    for (int r = warp; r < kTcRows; r += kTcThreads / 32) {
+      unsigned char* row0 = sA[buf];
+      bool on = X.flag[r] != 0;
+      if (on && M.bits) {
+        bool hit = false;
+        for (int w = 0; w < ms; ++w) hit |= (__ldg(pg + w) & X.gate[r][w]) != 0;
+        on = hit;
+      }
+      float acc[kTcRounds][4];
+#pragma unroll
+      for (int u = 0; u < kTcRounds; ++u)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[u][q] = 0.f;
+      bool any = false;
+      if (on) {
+        const int b = X.beg[r], n = X.len[r], e2 = b + span, s = X.sent[r];
+        const long long off = B.cell_off[s], toff = off + tri(n);
+        const int nsplit = job == IN_NN ? span - 1 : 1;
+        for (int ch = 0; ch < nsplit; ch += 32) {
+          const int i = ch + lane;
+          bool ok = false;
+          long long lc = 0, rc = 0;
+          if (i < nsplit) {
+            if (job == IN_NN) {
+              ok = (X.allow[r][i >> 5] >> (i & 31)) & 1;
+              lc = toff + chart_index(b, b + 1 + i, n);
+              rc = toff + chart_index(b + 1 + i, e2, n);
+            } else if (job == IN_NT) {
+              ok = X.allow1[r][0];
+              lc = toff + chart_index(b, e2 - 1, n);
+              rc = off + chart_index(e2 - 1, e2, n);
+            } else if (job == IN_TN) {
+              ok = X.allow1[r][1];
+              lc = off + chart_index(b, b + 1, n);
+              rc = toff + chart_index(b + 1, e2, n);
+            } else {
+              ok = X.allow1[r][2];
+              lc = off + chart_index(b, b + 1, n);
+              rc = off + chart_index(b + 1, e2, n);
+            }
+            ok = ok && live_bit(V.in, lc, ms, ca) && live_bit(V.in, rc, ms, cb);
+          }
+          const float scl = ok ? __expf(-X.ps[r] + scale_of(M.iscale, lc) + scale_of(M.iscale, rc)) : 0.f;
+          const unsigned m = __ballot_sync(kFull, ok);
+          if (m) any = true;
+          const int lci = (int)lc, rci = (int)rc;
+          for (unsigned mm = m; mm; mm &= mm - 1) {
+            const int sl = __ffs(mm) - 1;
+            const float* Ar = inside + (long long)__shfl_sync(kFull, lci, sl) * cs;
+            const float* Br = inside + (long long)__shfl_sync(kFull, rci, sl) * cs;
+            const float sc = __shfl_sync(kFull, scl, sl);
+#pragma unroll
+            for (int u = 0; u < kTcRounds; ++u) {
+              const int t = lane + 32 * u;
+              if (t < ntask) {
+                const int j = t / nkq, k0 = (t - j * nkq) * 4;
+                const float a = __ldg(Ar + __ldg(amem + a0 + j)) * sc;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                  if (k0 + q < nz) acc[u][q] = fmaf(a, __ldg(Br + __ldg(bmem + b0 + k0 + q)), acc[u][q]);
+              }
+            }
+          }
+        }
+      }
+      if (any) {
+#pragma unroll
+        for (int u = 0; u < kTcRounds; ++u) {
+          const int t = lane + 32 * u;
+          if (t < ntask) {
+            const int j = t / nkq, k0 = (t - j * nkq) * 4;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+              if (k0 + q < nz)
+                *reinterpret_cast<__nv_bfloat16*>(row0 + tc::tile_offset(r, j * nz + k0 + q, kpad)) =
+                    __float2bfloat16_rn(acc[u][q]);
+          }
+        }
+        for (int jk = kk + lane; jk < kpad; jk += 32)
+          *reinterpret_cast<__nv_bfloat16*>(row0 + tc::tile_offset(r, jk, kpad)) = __float2bfloat16_rn(0.f);
+        local_any = 1;
+      } else {
+        for (int c8 = lane; c8 < (kpad >> 3); c8 += 32)
+          *reinterpret_cast<uint4*>(row0 + ((r >> 3) * (kpad >> 3) + c8) * 128 + (r & 7) * 16) = make_uint4(0, 0, 0, 0);
+      }
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    const int any = __syncthreads_or(local_any);
+    tc::fence_after_sync();
+    if (!any) continue;
+    if (tid == 0) {
+      const uint32_t abase = tc::smem_u32(sA[buf]), bbase = tc::smem_u32(sB[buf]);
+      const uint32_t sbo = (uint32_t)kpad * 16, bstride = (uint32_t)T.slot_w * kpad * 2;
+      for (int i = 0; i < nb; ++i) {
+        const uint32_t d = taddr + (uint32_t)(__ldg(T.tblk + tp.z + i) * T.slot_w);
+        for (int k16 = 0; k16 < kpad / 16; ++k16)
+          tc::mma_bf16(d, tc::smem_desc(abase + k16 * 256, 128, sbo),
+                       tc::smem_desc(bbase + i * bstride + k16 * 256, 128, sbo), idesc, 1u);
+      }
+      tc::mma_commit(&X.bar[buf]);
+    }
+    ++ncommit[buf];
+    ++it;
+    issued = true;
+  }
+  // --- read out ---------------------------------------------------------------
+  if (issued) {
+    if (tid == 0) tc::mma_commit(&X.bar_fin);
+    if (!tc::mbar_wait(&X.bar_fin, 0, kWaitNs)) {
+      atomicExch(&X.err, 1);
+      atomicExch(T.err, 1);
+    }
+  }
+  tc::fence_after_sync();
+  __syncthreads();
+  const bool failed = X.err != 0;
+  {
+    const int q = warp & 3, chunk = warp >> 2, per = T.ncols / 4, r = q * 32 + lane;
+    const bool mine = X.flag[r] && !failed;
+    for (int c = chunk * per; c < (chunk + 1) * per; c += 16) {
+      float v[16];
+      tc::tmem_ld16(taddr + ((uint32_t)(q * 32) << 16) + c, v);
+      if (!mine) continue;
+      float* row = inside + X.pbot[r] * cs;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int t = __ldg(T.col_tgt + h * T.ncols + c + i);
+        if (t < 0) continue;
+        bool g = true;
+        if (M.bits) {
+          g = false;
+          for (int w = 0; w < ms; ++w) g |= (__ldg(T.tgt_gate + t * ms + w) & X.gate[r][w]) != 0;
+        }
+        row[t] = g ? v[i] : 0.f;
+      }
+    }
+    if (h == 0 && chunk == 0 && mine)
+      for (int u = 0; u < T.n_uncovered; ++u) inside[X.pbot[r] * cs + __ldg(T.uncovered + u)] = 0.f;
+    if (failed && tid < kTcRows && X.flag[tid] && C.status) C.status[X.sent[tid]] = 5;  // PUCK_ERR_DEVICE_TIMEOUT
+  }
+  // a failed wait: the MMAs may still be running; give them another bounded
+  // wait before the columns are freed
+  if (failed && issued) tc::mbar_wait(&X.bar_fin, 0, kWaitNs);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, T.ncols);
+}
+
 }  // namespace
+
+size_t tc_static_smem_bytes() { return sizeof(TcCells); }
+
+size_t tc_smem_bytes(const DevTc& T) { return 2 * (size_t)kTcRows * T.max_kpad * 2 + 2 * (size_t)T.bcap; }
+
+cudaError_t launch_inside_tc(const DevLevel& L, const DevTc& T, const DevBatch& B, int span, const int* cells,
+                             int ncells, const DevMask& M, float* inside, DevLive V, Counters C, cudaStream_t st) {
+  if (ncells <= 0 || span < 2) return cudaSuccess;
+  const size_t smem = tc_smem_bytes(T);
+  if (cudaError_t e = cudaFuncSetAttribute(k_inside_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      e != cudaSuccess)
+    return e;
+  const dim3 grid((unsigned)((ncells + kTcRows - 1) / kTcRows), (unsigned)T.nparts);
+  k_inside_tc<<<grid, kTcThreads, smem, st>>>(L, T, B, span, cells, ncells, M, inside, V, C);
+  return cudaGetLastError();
+}
+
 }  // namespace puck
 
 extern "C" puck_status puck_tc_selftest(int32_t device, int32_t k, int32_t n, const uint16_t* a, const uint16_t* b,

@@ -186,7 +186,8 @@ class CLParser:
 
     def __init__(self, grammar_path: str, max_alloc_size: int = 1 << 30, profile: bool = False,
                  device: int = 0, decode: str = "auto", max_length: int = 100,
-                 prune_threshold: float = -9.0, max_batch_sentences: int = 0, use_graphs: bool = False):
+                 prune_threshold: float = -9.0, max_batch_sentences: int = 0, use_graphs: bool = False,
+                 tensor_cores: bool = False):
         L = _lib.load()
         st = ctypes.c_int32(0)
         self._g = L.puck_grammar_load(grammar_path.encode(), ctypes.byref(st))
@@ -203,6 +204,7 @@ class CLParser:
         opt.prune_threshold = prune_threshold
         opt.max_batch_sentences = max_batch_sentences
         opt.use_graphs = 1 if use_graphs else 0
+        opt.tensor_cores = 1 if tensor_cores else 0
         self.max_length = max_length
         self._p = L.puck_parser_create(self._g, ctypes.byref(opt), ctypes.byref(st))
         if not self._p:
@@ -323,6 +325,15 @@ class CLParser:
         _lib.check(self._L.puck_parser_autotune(self._p, _ptr(words), _ptr(offsets), len(offsets) - 1, _ptr(out)))
         names = {0: "target-major", 2: "pair-factored"}
         return {"levels": [names.get(int(m), str(int(m))) for m in out[:nl]], "waves": int(out[nl]) / 100.0}
+
+    def tensor_cores(self, level: int):
+        """(True, "") if the level's inside binary sums run on tensor cores,
+        else (False, reason)."""
+        buf = ctypes.create_string_buffer(256)
+        r = self._L.puck_parser_tensor_cores(self._p, level, buf, 256)
+        if r < 0:
+            raise ValueError(f"bad level {level}")
+        return r == 1, buf.value.decode()
 
     def level_work(self, level: int):
         """(binary work units, +0.0 partials) of one level in the last call."""
