@@ -432,7 +432,9 @@ def run_mbr(args):
     torch.cuda.set_device(0)
     levels, path, sents = workload(args.seed, args.sentences, fine_semiring="real")
     words, offsets, _ = pack_sentences(sents)
-    P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, max_length=MAX_LEN, decode="mbr")
+    P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, max_length=MAX_LEN, decode="mbr",
+                 tensor_cores=args.tensor_cores)
+    tc_on, tc_why = P.tensor_cores(len(levels) - 1)
     for _ in range(args.warmup):
         nodes, st = P.parse_ids(words, offsets)
     assert (st == 0).all()
@@ -487,10 +489,14 @@ def run_mbr(args):
         "metric": "MBR sentences/sec, 1.1k-symbol split grammar, sum-product (Real) fine level, len<=40",
         "value": round(value, 2), "unit": "sentences/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(sum(dev_ms) / len(dev_ms), 3), "higher_is_better": True,
-        "dtype": "f32", "data": "synthetic (seeded split grammar and sentences with the published shapes)",
+        "dtype": "bf16 x bf16 -> f32 (inside binary sums), f32 elsewhere" if tc_on else "f32",
+        "data": "synthetic (seeded split grammar and sentences with the published shapes)",
         "config": {"workload": "split-grammar cascade: coarse Viterbi, masks at -9, fine Real inside/outside, "
                                f"MBR trees; {args.sentences} sentences lognormal(mean 23) clipped 1-40",
-                   "path": "FP32 CUDA cores (pair-factored sum-product)"},
+                   "path": ("fine inside binary sums on tcgen05 tensor cores (BF16 operands, FP32 TMEM "
+                            "accumulation); outside pass and the rest FP32 CUDA cores") if tc_on else
+                           "FP32 CUDA cores (pair-factored sum-product)" + (f"; tensor cores: {tc_why}" if
+                                                                           args.tensor_cores else "")},
         "e2e": {"value": round(args.sentences * len(api_ms) / (sum(api_ms) / 1e3), 2), "unit": "sentences/s"},
         "clocks": clk.summary(), "passes_ms_last_step": passes,
         "errors_vs_fp64": {
@@ -609,6 +615,8 @@ def main():
     ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x], default="1000,2000,3000")
     ap.add_argument("--serve-sentences", type=int, default=6000)
     ap.add_argument("--serve-mem-gb", type=int, default=32)
+    ap.add_argument("--tensor-cores", action="store_true",
+                    help="mbr config: the fine level's inside binary sums on tcgen05 tensor cores (BF16)")
     ap.add_argument("--config", default="viterbi", choices=["viterbi", "mbr", "long", "small"],
                     help="viterbi: the headline batched/served Viterbi cascade (default); mbr: sum-product "
                          "MBR throughput and errors against FP64; long: long sentences on a ~2k-symbol grammar; "

@@ -195,7 +195,7 @@ size_t pass_smem_bytes(const DevLevel& L, int chunk);
 // TMEM part.  The cells are finished by launch_inside_span with
 // L.tc_binary set.
 constexpr int kTcRows = 128;
-constexpr int kTcThreads = 512;
+constexpr int kTcThreads = 1024;
 size_t tc_smem_bytes(const DevTc& T);
 size_t tc_static_smem_bytes();
 cudaError_t launch_inside_tc(const DevLevel& L, const DevTc& T, const DevBatch& B, int span, const int* cells,

@@ -513,6 +513,9 @@ bool puck_host::build_tc(LevelDev& D, const HostLevel& L, std::string* why) {
       const int ca = J.pk[p] & 255, cb = (J.pk[p] >> 8) & 255;
       const int kk = (J.ao[ca + 1] - J.ao[ca]) * (J.bo[cb + 1] - J.bo[cb]);
       if (kk > 256) return no("a coarse pair with more than 256 child pairs");
+      if ((J.ao[ca + 1] - J.ao[ca]) * ((J.bo[cb + 1] - J.bo[cb] + 3) / 4) > 96 || J.ao[ca + 1] - J.ao[ca] > 32 ||
+          J.bo[cb + 1] - J.bo[cb] > 32)
+        return no("a coarse pair's outer product exceeds three tasks per lane");
       max_kpad = std::max(max_kpad, (kk + 15) / 16 * 16);
       for (int b = J.pbk[p]; b < J.pbk[p + 1]; ++b) {
         const std::vector<int> bits(J.sb + (size_t)J.bs[b] * ms, J.sb + (size_t)(J.bs[b] + 1) * ms);
@@ -537,7 +540,9 @@ bool puck_host::build_tc(LevelDev& D, const HostLevel& L, std::string* why) {
   const int per_part_max = 512 / slot_w;
   const int nparts = ((int)parents.size() + per_part_max - 1) / per_part_max;
   const int per_part = ((int)parents.size() + nparts - 1) / nparts;
-  int ncols = 64;  // a multiple of 64: four warps zero and read a quarter each, 16 columns at a time
+  // each group of four warps zeroes and reads its share of the columns, 16 at
+  // a time: a multiple of 16 per group
+  int ncols = 16 * (puck::kTcThreads / 128);
   while (ncols < per_part * slot_w) ncols <<= 1;
   std::vector<int> part_of(L.n_coarse, -1), slot_of(L.n_coarse, -1);
   std::vector<int> col_tgt((size_t)nparts * ncols, -1);
@@ -559,11 +564,11 @@ bool puck_host::build_tc(LevelDev& D, const HostLevel& L, std::string* why) {
   const size_t abytes = 2 * (size_t)puck::kTcRows * max_kpad * 2;
   const size_t blk_bytes = (size_t)slot_w * max_kpad * 2;
   if (abytes + static_smem + 2 * blk_bytes > 227 * 1024) return no("outer-product tiles too large for shared memory");
-  size_t bcap = std::min<size_t>(40 * 1024, (227 * 1024 - static_smem - abytes) / 2);
+  size_t bcap = std::min<size_t>(40 * 1024, (227 * 1024 - static_smem - abytes) / 2) / 128 * 128;
   // a CTA holding more than half of TMEM keeps its SM to itself (a second
   // one would wait in tcgen05.alloc): shared memory for one CTA per SM
-  if (ncols > 256 && abytes + 2 * bcap + static_smem < 120 * 1024) bcap = (120 * 1024 - abytes - static_smem + 1) / 2;
-  bcap = (bcap + 127) / 128 * 128;
+  if (ncols > 256 && abytes + 2 * bcap + static_smem < 120 * 1024)
+    bcap = ((120 * 1024 - abytes - static_smem + 1) / 2 + 127) / 128 * 128;
   if (abytes + 2 * bcap + static_smem > 227 * 1024) return no("tensor-core buffers do not fit shared memory");
   // Entries, per part, job and pair: the pair's freely gated rules, then one
   // entry per segment for rules of targets with differing segments.  An

@@ -104,16 +104,49 @@ struct TcCells {
   int gate[kTcRows][kMaxMask];
   unsigned allow[kTcRows][kMaxLen / 32];    // NN: split b + 1 + i has both operand cells unpruned
   unsigned char allow1[kTcRows][4];         // NT, TN, TT
+  unsigned m[kTcRows][kMaxLen / 32];        // this pair's live splits per cell
+  int live[kTcRows];
   uint32_t taddr;
   int err;
   uint64_t bar[2], bar_fin;
 };
 
-constexpr int kTcRounds = 4;  // outer-product tasks per lane (ny * ceil(nz / 4) <= 128)
-
 __device__ __forceinline__ bool live_bit(const int* live, long long cell, int ms, int c) {
   return (__ldg(live + cell * ms + (c >> 5)) >> (c & 31)) & 1;
 }
+
+// Operand cells of split i of cell r for a job; false if the split is out of
+// range or not allowed (an operand cell pruned).
+__device__ __forceinline__ bool split_cells(const TcCells& X, const DevBatch& B, int r, int job, int span, int i,
+                                            int nsplit, long long& lc, long long& rc) {
+  using namespace dev;
+  lc = rc = 0;
+  if (i >= nsplit) return false;
+  const int b = X.beg[r], n = X.len[r], e = b + span;
+  const long long off = B.cell_off[X.sent[r]], toff = off + tri(n);
+  if (job == IN_NN) {
+    lc = toff + chart_index(b, b + 1 + i, n);
+    rc = toff + chart_index(b + 1 + i, e, n);
+    return (X.allow[r][i >> 5] >> (i & 31)) & 1;
+  }
+  if (job == IN_NT) {
+    lc = toff + chart_index(b, e - 1, n);
+    rc = off + chart_index(e - 1, e, n);
+    return X.allow1[r][0];
+  }
+  lc = off + chart_index(b, b + 1, n);
+  if (job == IN_TN) {
+    rc = toff + chart_index(b + 1, e, n);
+    return X.allow1[r][1];
+  }
+  rc = off + chart_index(b + 1, e, n);
+  return X.allow1[r][2];
+}
+
+constexpr int kTcRounds = 3;  // outer-product tasks per lane: ny * ceil(nz / 4) <= 96
+
+// per warp: two splits' staged member values of A_s and B_s
+__shared__ __align__(16) float g_stage[kTcThreads / 32][2][2][32];
 
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_inside_tc(DevLevel L, DevTc T, DevBatch B, int span, const int* cells, int ncells, DevMask M, float* inside,
@@ -174,7 +207,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const uint32_t taddr = X.taddr;
   // --- zero the accumulator --------------------------------------------------
   {
-    const int q = warp & 3, chunk = warp >> 2, per = T.ncols / 4;
+    const int q = warp & 3, chunk = warp >> 2, per = T.ncols / (kTcThreads / 128);
     for (int c = chunk * per; c < (chunk + 1) * per; c += 16) tc::tmem_st16_zero(taddr + ((uint32_t)(q * 32) << 16) + c);
     tc::tmem_wait_st();
   }
@@ -215,93 +248,147 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int b0 = __ldg(boff + cb), nz = __ldg(boff + cb + 1) - b0;
     const int kk = ny * nz, nkq = (nz + 3) >> 2, ntask = ny * nkq;
     const int* pg = T.tpair_gate + (size_t)e * ms;
-    int local_any = 0;
-    for (int r = warp; r < kTcRows; r += kTcThreads / 32) {
-      unsigned char* row0 = sA[buf];
-      bool on = X.flag[r] != 0;
-      if (on && M.bits) {
-        bool hit = false;
-        for (int w = 0; w < ms; ++w) hit |= (__ldg(pg + w) & X.gate[r][w]) != 0;
-        on = hit;
+    // phase 1: per cell, the live splits of this pair.  A warp takes eight
+    // cells and issues all their liveness loads before the first ballot.
+    unsigned pgw[kMaxMask];
+#pragma unroll
+    for (int w = 0; w < kMaxMask; ++w) pgw[w] = w < ms ? (unsigned)__ldg(pg + w) : 0u;
+    {
+      constexpr int kPer = kTcRows / (kTcThreads / 32);
+      const int nsplit = job == IN_NN ? span - 1 : 1;
+      for (int ch = 0; ch < nsplit; ch += 32) {
+        bool ok[kPer];
+        int lw[kPer], rw[kPer];
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+          const int r = warp * kPer + i;
+          bool on = X.flag[r] != 0;
+          if (on && M.bits) {
+            bool hit = false;
+#pragma unroll
+            for (int w = 0; w < kMaxMask; ++w) hit |= w < ms && (pgw[w] & (unsigned)X.gate[r][w]) != 0;
+            on = hit;
+          }
+          long long lc = 0, rc = 0;
+          ok[i] = on && split_cells(X, B, r, job, span, ch + lane, nsplit, lc, rc);
+          lw[i] = ok[i] ? __ldg(V.in + lc * ms + (ca >> 5)) : 0;
+          rw[i] = ok[i] ? __ldg(V.in + rc * ms + (cb >> 5)) : 0;
+        }
+#pragma unroll
+        for (int i = 0; i < kPer; ++i) {
+          const int r = warp * kPer + i;
+          const unsigned m = __ballot_sync(kFull, ok[i] && ((lw[i] >> (ca & 31)) & 1) && ((rw[i] >> (cb & 31)) & 1));
+          if (lane == 0) {
+            X.m[r][ch >> 5] = m;
+            X.live[r] = (ch == 0 ? 0 : X.live[r]) | (m != 0);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // phase 2: (live cell, task round) items over all warps; dead rows zeroed
+    unsigned lm[kTcRows / 32];
+    int nlive = 0;
+#pragma unroll
+    for (int i = 0; i < kTcRows / 32; ++i) {
+      lm[i] = __ballot_sync(kFull, X.live[i * 32 + lane] != 0);
+      nlive += __popc(lm[i]);
+    }
+    // the pair's member indices, one per lane (rows of A_s and B_s it stages)
+    const int my_a = lane < ny ? __ldg(amem + a0 + lane) : -1;
+    const int my_b = lane < nz ? __ldg(bmem + b0 + lane) : -1;
+    const int nrounds = (ntask + 31) >> 5;
+    float(*stg)[2][32] = g_stage[warp];  // [split][A or B][member]
+    for (int k = warp; k < nlive; k += kTcThreads / 32) {
+      int r = 0;
+      for (int i = 0, acc0 = 0; i < kTcRows / 32; ++i) {
+        const int c = __popc(lm[i]);
+        if (k < acc0 + c) {
+          unsigned mm = lm[i];
+          for (int z = acc0; z < k; ++z) mm &= mm - 1;  // drop the live cells before the k-th
+          r = i * 32 + __ffs(mm) - 1;
+          break;
+        }
+        acc0 += c;
       }
       float acc[kTcRounds][4];
 #pragma unroll
       for (int u = 0; u < kTcRounds; ++u)
 #pragma unroll
         for (int q = 0; q < 4; ++q) acc[u][q] = 0.f;
-      bool any = false;
-      if (on) {
-        const int b = X.beg[r], n = X.len[r], e2 = b + span, s = X.sent[r];
-        const long long off = B.cell_off[s], toff = off + tri(n);
-        const int nsplit = job == IN_NN ? span - 1 : 1;
-        for (int ch = 0; ch < nsplit; ch += 32) {
-          const int i = ch + lane;
-          bool ok = false;
-          long long lc = 0, rc = 0;
-          if (i < nsplit) {
-            if (job == IN_NN) {
-              ok = (X.allow[r][i >> 5] >> (i & 31)) & 1;
-              lc = toff + chart_index(b, b + 1 + i, n);
-              rc = toff + chart_index(b + 1 + i, e2, n);
-            } else if (job == IN_NT) {
-              ok = X.allow1[r][0];
-              lc = toff + chart_index(b, e2 - 1, n);
-              rc = off + chart_index(e2 - 1, e2, n);
-            } else if (job == IN_TN) {
-              ok = X.allow1[r][1];
-              lc = off + chart_index(b, b + 1, n);
-              rc = toff + chart_index(b + 1, e2, n);
-            } else {
-              ok = X.allow1[r][2];
-              lc = off + chart_index(b, b + 1, n);
-              rc = off + chart_index(b + 1, e2, n);
-            }
-            ok = ok && live_bit(V.in, lc, ms, ca) && live_bit(V.in, rc, ms, cb);
-          }
-          const float scl = ok ? __expf(-X.ps[r] + scale_of(M.iscale, lc) + scale_of(M.iscale, rc)) : 0.f;
-          const unsigned m = __ballot_sync(kFull, ok);
-          if (m) any = true;
-          const int lci = (int)lc, rci = (int)rc;
-          for (unsigned mm = m; mm; mm &= mm - 1) {
-            const int sl = __ffs(mm) - 1;
-            const float* Ar = inside + (long long)__shfl_sync(kFull, lci, sl) * cs;
-            const float* Br = inside + (long long)__shfl_sync(kFull, rci, sl) * cs;
-            const float sc = __shfl_sync(kFull, scl, sl);
+      const int nsplit = job == IN_NN ? span - 1 : 1;
+      for (int ch = 0; ch < nsplit; ch += 32) {
+        const unsigned m = X.m[r][ch >> 5];
+        if (!m) continue;
+        long long lc = 0, rc = 0;
+        float scl = 0.f;
+        if ((m >> lane) & 1) {
+          split_cells(X, B, r, job, span, ch + lane, nsplit, lc, rc);
+          scl = __expf(-X.ps[r] + scale_of(M.iscale, lc) + scale_of(M.iscale, rc));
+        }
+        const int lci = (int)lc, rci = (int)rc;
+        // two live splits per step: each lane stages one member value of
+        // A_s and of B_s (scaled), then computes its tasks from shared memory
+        for (unsigned mm = m; mm;) {
+          const int s0 = __ffs(mm) - 1;
+          mm &= mm - 1;
+          const bool two = mm != 0;
+          const int s1 = two ? __ffs(mm) - 1 : s0;
+          if (two) mm &= mm - 1;
+          const long long L0 = __shfl_sync(kFull, lci, s0), R0 = __shfl_sync(kFull, rci, s0);
+          const long long L1 = __shfl_sync(kFull, lci, s1), R1 = __shfl_sync(kFull, rci, s1);
+          const float sc0 = __shfl_sync(kFull, scl, s0), sc1 = __shfl_sync(kFull, scl, s1);
+          const float av0 = my_a >= 0 ? __ldg(inside + L0 * cs + my_a) * sc0 : 0.f;
+          const float bv0 = my_b >= 0 ? __ldg(inside + R0 * cs + my_b) : 0.f;
+          const float av1 = two && my_a >= 0 ? __ldg(inside + L1 * cs + my_a) * sc1 : 0.f;
+          const float bv1 = two && my_b >= 0 ? __ldg(inside + R1 * cs + my_b) : 0.f;
+          stg[0][0][lane] = av0;
+          stg[0][1][lane] = bv0;
+          stg[1][0][lane] = av1;
+          stg[1][1][lane] = bv1;
+          __syncwarp();
 #pragma unroll
-            for (int u = 0; u < kTcRounds; ++u) {
-              const int t = lane + 32 * u;
-              if (t < ntask) {
-                const int j = t / nkq, k0 = (t - j * nkq) * 4;
-                const float a = __ldg(Ar + __ldg(amem + a0 + j)) * sc;
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                  if (k0 + q < nz) acc[u][q] = fmaf(a, __ldg(Br + __ldg(bmem + b0 + k0 + q)), acc[u][q]);
-              }
+          for (int u = 0; u < kTcRounds; ++u) {
+            const int t = lane + 32 * u;
+            if (u < nrounds && t < ntask) {
+              const int j = t / nkq, k0 = (t - j * nkq) * 4;
+              const float x0 = stg[0][0][j], x1 = stg[1][0][j];
+              const float4 y0 = *reinterpret_cast<const float4*>(&stg[0][1][k0]);
+              const float4 y1 = *reinterpret_cast<const float4*>(&stg[1][1][k0]);
+              acc[u][0] = fmaf(x1, y1.x, fmaf(x0, y0.x, acc[u][0]));
+              acc[u][1] = fmaf(x1, y1.y, fmaf(x0, y0.y, acc[u][1]));
+              acc[u][2] = fmaf(x1, y1.z, fmaf(x0, y0.z, acc[u][2]));
+              acc[u][3] = fmaf(x1, y1.w, fmaf(x0, y0.w, acc[u][3]));
             }
           }
+          __syncwarp();
         }
       }
-      if (any) {
+      unsigned char* row0 = sA[buf];
 #pragma unroll
-        for (int u = 0; u < kTcRounds; ++u) {
-          const int t = lane + 32 * u;
-          if (t < ntask) {
-            const int j = t / nkq, k0 = (t - j * nkq) * 4;
+      for (int u = 0; u < kTcRounds; ++u) {
+        const int t = lane + 32 * u;
+        if (u < nrounds && t < ntask) {
+          const int j = t / nkq, k0 = (t - j * nkq) * 4;
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (k0 + q < nz)
-                *reinterpret_cast<__nv_bfloat16*>(row0 + tc::tile_offset(r, j * nz + k0 + q, kpad)) =
-                    __float2bfloat16_rn(acc[u][q]);
-          }
+          for (int q = 0; q < 4; ++q)
+            if (k0 + q < nz)
+              *reinterpret_cast<__nv_bfloat16*>(row0 + tc::tile_offset(r, j * nz + k0 + q, kpad)) =
+                  __float2bfloat16_rn(acc[u][q]);
         }
-        for (int jk = kk + lane; jk < kpad; jk += 32)
-          *reinterpret_cast<__nv_bfloat16*>(row0 + tc::tile_offset(r, jk, kpad)) = __float2bfloat16_rn(0.f);
-        local_any = 1;
-      } else {
-        for (int c8 = lane; c8 < (kpad >> 3); c8 += 32)
-          *reinterpret_cast<uint4*>(row0 + ((r >> 3) * (kpad >> 3) + c8) * 128 + (r & 7) * 16) = make_uint4(0, 0, 0, 0);
+      }
+      for (int jk = kk + lane; jk < kpad; jk += 32)
+        *reinterpret_cast<__nv_bfloat16*>(row0 + tc::tile_offset(r, jk, kpad)) = __float2bfloat16_rn(0.f);
+    }
+    {
+      const int c8n = kpad >> 3;
+      for (int i = tid; i < kTcRows * c8n; i += kTcThreads) {
+        const int r = i / c8n, c8 = i - r * c8n;
+        if (!X.live[r])
+          *reinterpret_cast<uint4*>(sA[buf] + ((r >> 3) * c8n + c8) * 128 + (r & 7) * 16) = make_uint4(0, 0, 0, 0);
       }
     }
+    const int local_any = nlive > 0;
     tc::fence_async_smem();
     tc::fence_before_sync();
     const int any = __syncthreads_or(local_any);
@@ -334,7 +421,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   const bool failed = X.err != 0;
   {
-    const int q = warp & 3, chunk = warp >> 2, per = T.ncols / 4, r = q * 32 + lane;
+    const int q = warp & 3, chunk = warp >> 2, per = T.ncols / (kTcThreads / 128), r = q * 32 + lane;
     const bool mine = X.flag[r] && !failed;
     for (int c = chunk * per; c < (chunk + 1) * per; c += 16) {
       float v[16];
@@ -367,7 +454,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
 }  // namespace
 
-size_t tc_static_smem_bytes() { return sizeof(TcCells); }
+size_t tc_static_smem_bytes() { return sizeof(TcCells) + sizeof(g_stage); }
 
 size_t tc_smem_bytes(const DevTc& T) { return 2 * (size_t)kTcRows * T.max_kpad * 2 + 2 * (size_t)T.bcap; }
 
