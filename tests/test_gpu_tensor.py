@@ -42,13 +42,6 @@ def test_tc_tile_product_matches_host(k, n):
     assert err.max() < 1e-5, (err.max(), np.unravel_index(err.argmax(), err.shape))
 
 
-def test_tc_selftest_rejects_bad_shapes():
-    L = _lib.load()
-    z = np.zeros(128 * 32, np.uint16)
-    d = np.zeros(128 * 32, np.float32)
-    assert L.puck_tc_selftest(0, 24, 16, z.ctypes.data, z.ctypes.data, d.ctypes.data) == 6
-    assert L.puck_tc_selftest(0, 16, 8, z.ctypes.data, z.ctypes.data, d.ctypes.data) == 6
-
 
 # --- the sum-product inside pass on tensor cores ------------------------------
 # BF16 operands (outer products and rule weights) with FP32 accumulation:

@@ -28,6 +28,26 @@ def test_library_exports_every_declared_symbol():
     assert set(names) >= set(_lib.EXPORTS)
 
 
+def test_options_layout_and_defaults():
+    """The ctypes mirror of puck_options has the C layout (40 bytes, no
+    padding after tensor_cores) and the library's defaults."""
+    L = _lib.load()
+    assert ctypes.sizeof(_lib.Options) == 40
+    assert _lib.Options.tensor_cores.offset == 36
+    opt = _lib.Options()
+    opt.tensor_cores = 7
+    L.puck_default_options(ctypes.byref(opt))
+    assert opt.tensor_cores == 0 and opt.use_graphs == 0 and abs(opt.prune_threshold + 9.0) < 1e-6
+
+
+def test_tc_selftest_rejects_bad_shapes_without_a_device_call():
+    L = _lib.load()
+    z = np.zeros(128 * 32, np.uint16)
+    d = np.zeros(128 * 32, np.float32)
+    for k, n in ((24, 16), (16, 8), (0, 16), (272, 16), (16, 272)):
+        assert L.puck_tc_selftest(0, k, n, z.ctypes.data, z.ctypes.data, d.ctypes.data) == 6
+
+
 def test_grammar_load_and_queries_on_host():
     L = _lib.load()
     st = ctypes.c_int32(-1)
