@@ -358,6 +358,26 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         // lane l runs its contiguous, target-sorted slice of the block; the
         // slices are stored interleaved, so each step's loads are coalesced
         const int r0 = __ldg(J.blk_ptr + bk), per = (__ldg(J.blk_ptr + bk + 1) - r0) >> 5;
+        if (J.interleaved == 2) {
+          // every rule of the lane's slice has the same target: one running
+          // max, flushed once (padding rules carry the zero weight)
+          float best = Sr<S>::zero();
+          int tl = 0;
+          for (int i0 = 0; i0 < per; i0 += kRuleBatch) {
+            int2 R[kRuleBatch];
+#pragma unroll
+            for (int q = 0; q < kRuleBatch; ++q) R[q] = __ldg(J.pair_rules + r0 + (i0 + q) * 32 + lane);
+            float m4[kRuleBatch];
+#pragma unroll
+            for (int q = 0; q < kRuleBatch; ++q) m4[q] = Mw[R[q].x & 0xffff];
+#pragma unroll
+            for (int q = 0; q < kRuleBatch; ++q) best = Sr<S>::add(best, m4[q] + __int_as_float(R[q].y));
+            tl = (int)((unsigned)R[0].x >> 16);
+          }
+          flush_run<S>(P, tl, best, corner);
+          if (lane == 0) work += (unsigned long long)__ldg(J.blk_nrule + bk);
+          continue;
+        }
         // kRuleBatch rules per step: their loads are issued before any is used
         // (the step count `per` is the same for every lane of the warp)
         for (int i0 = 0; i0 < per; i0 += kRuleBatch) {

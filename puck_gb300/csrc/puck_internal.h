@@ -35,7 +35,9 @@ struct DevJob {
   // with j, k the operands' positions among their coarse symbol's members.
   int npair;
   int a_is_t, b_is_t;
-  int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs)
+  int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs):
+                          // 1 mixed-target slices, 2 one target per lane slice (slice length a
+                          // multiple of 4)
   const int* pair_key;    // [npair] ca | cb << 8
   const int* pair_gate;   // [npair * mask_size] OR of the pair's segment bits
   const int* pair_blk;    // [npair + 1] block range

@@ -368,32 +368,96 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
       dev_bp.assign(bp, bp + nbp);
       for (int64_t b = 0; b + 1 < nbp; ++b) blk_n.push_back(bp[b + 1] - bp[b]);
     }
+    // Viterbi inside jobs: each lane's slice holds rules of one target only
+    // (per-target lanes), so the kernel keeps one running max per lane and
+    // flushes it once.  A target gets lanes in proportion to its rules; the
+    // slice length is padded to a multiple of four.  Blocks with more than 32
+    // targets keep mixed slices (the job then uses the run-tracking loop).
+    bool one_target_lanes = interleave;
+    for (int64_t b = 0; one_target_lanes && b + 1 < nbp; ++b) {
+      int ntg = 0;
+      for (int r = bp[b]; r < bp[b + 1]; ++r)
+        ntg += r == bp[b] || ((unsigned)pr[r] >> 16) != ((unsigned)pr[r - 1] >> 16);
+      if (ntg > 32) one_target_lanes = false;
+    }
     for (int64_t b = 0; interleave && b + 1 < nbp; ++b) {
-      const int r0 = bp[b], cnt = bp[b + 1] - bp[b], per = (cnt + 31) / 32, nz = blk_nz[b];
-      const size_t base = rr.size();
-      rr.resize(base + (size_t)per * 32);
+      const int r0 = bp[b], cnt = bp[b + 1] - bp[b], nz = blk_nz[b];
       auto tile_form = [nz](int x) {
         const int jj = x & 255, kk = (x >> 8) & 255;
         return (jj * nz + kk) | (x & ~0xffff);
       };
-      for (int slot = 0; slot < per * 32; ++slot) {
-        const int lane = slot % 32, i = slot / 32, logical = lane * per + i;
-        int2 v;
-        if (logical < cnt) {
-          v.x = tile_form(pr[r0 + logical]);
-          std::memcpy(&v.y, &pw[r0 + logical], 4);
-        } else {
-          v.x = cnt ? (pr[r0 + cnt - 1] & ~0xffff) : 0;  // target kept, operand entry 0
-          std::memcpy(&v.y, &zero, 4);
+      const size_t base = rr.size();
+      if (one_target_lanes) {
+        // targets of the block (its rules are sorted by target) and their lanes
+        std::vector<int> tstart, tcnt, tlanes;
+        for (int r = 0; r < cnt; ++r)
+          if (r == 0 || ((unsigned)pr[r0 + r] >> 16) != ((unsigned)pr[r0 + r - 1] >> 16)) {
+            tstart.push_back(r);
+            tcnt.push_back(0);
+          }
+        for (size_t k = 0; k < tstart.size(); ++k)
+          tcnt[k] = (k + 1 < tstart.size() ? tstart[k + 1] : cnt) - tstart[k];
+        tlanes.assign(tstart.size(), 1);
+        int free_lanes = 32 - (int)tstart.size();
+        auto slice = [&](size_t k) { return (tcnt[k] + tlanes[k] - 1) / tlanes[k]; };
+        while (free_lanes > 0 && !tstart.empty()) {
+          size_t best = 0;
+          for (size_t k = 1; k < tstart.size(); ++k)
+            if (slice(k) > slice(best)) best = k;
+          if (slice(best) <= 1) break;
+          ++tlanes[best];
+          --free_lanes;
         }
-        rr[base + slot] = v;
+        int per = 0;
+        for (size_t k = 0; k < tstart.size(); ++k) per = std::max(per, slice(k));
+        per = (per + 3) / 4 * 4;
+        rr.resize(base + (size_t)per * 32);
+        const int pad_t = cnt ? (pr[r0] & ~0xffff) : 0;
+        for (size_t slot = 0; slot < (size_t)per * 32; ++slot) {
+          rr[base + slot].x = pad_t;  // a valid target, operand entry 0, zero weight
+          std::memcpy(&rr[base + slot].y, &zero, 4);
+        }
+        int lane = 0;
+        for (size_t k = 0; k < tstart.size(); ++k) {
+          const int len = slice(k);
+          for (int l = 0; l < tlanes[k]; ++l, ++lane) {
+            const int a0 = tstart[k] + l * len, a1 = std::min(tstart[k] + tcnt[k], a0 + len);
+            const int tpad = pr[r0 + tstart[k]] & ~0xffff;
+            for (int i = 0; i < per; ++i) {
+              int2 v;
+              if (a0 + i < a1) {
+                v.x = tile_form(pr[r0 + a0 + i]);
+                std::memcpy(&v.y, &pw[r0 + a0 + i], 4);
+              } else {
+                v.x = tpad;
+                std::memcpy(&v.y, &zero, 4);
+              }
+              rr[base + (size_t)i * 32 + lane] = v;
+            }
+          }
+        }
+      } else {
+        const int per = (cnt + 31) / 32;
+        rr.resize(base + (size_t)per * 32);
+        for (int slot = 0; slot < per * 32; ++slot) {
+          const int lane = slot % 32, i = slot / 32, logical = lane * per + i;
+          int2 v;
+          if (logical < cnt) {
+            v.x = tile_form(pr[r0 + logical]);
+            std::memcpy(&v.y, &pw[r0 + logical], 4);
+          } else {
+            v.x = cnt ? (pr[r0 + cnt - 1] & ~0xffff) : 0;  // target kept, operand entry 0
+            std::memcpy(&v.y, &zero, 4);
+          }
+          rr[base + slot] = v;
+        }
       }
       dev_bp.push_back((int)rr.size());
       blk_n.push_back(cnt);
     }
     if (rr.size() > (size_t)INT32_MAX) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule table too large in " + n};
     J.npair = (int)npk;
-    J.interleaved = interleave ? 1 : 0;
+    J.interleaved = !interleave ? 0 : one_target_lanes ? 2 : 1;
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
