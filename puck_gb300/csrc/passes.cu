@@ -65,6 +65,7 @@ struct Smem {
   float* stA;
   float* stB;
   float* M;
+  float* stage;  // per warp 128 floats: two splits' staged A and B members (16-byte aligned)
   unsigned* pl;
   int* list;
 };
@@ -75,10 +76,12 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk)
   m.P = base;
   m.Q = base + cs;
   float* rest = base + 2 * cs;
-  m.stA = m.stB = m.M = nullptr;
+  m.stA = m.stB = m.M = m.stage = nullptr;
   m.pl = nullptr;
   m.list = nullptr;
   if (L.mode == 2) {
+    m.stage = rest;
+    rest += (blockDim.x >> 5) * 128;
     m.M = rest;
     m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * L.max_mtile);
     m.list = reinterpret_cast<int*>(m.pl + L.n_coarse * L.mask_size);
@@ -268,6 +271,56 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       const int a0 = __ldg(aoff + ca), ny = __ldg(aoff + ca + 1) - a0;
       const int b0 = __ldg(boff + cb), nz = __ldg(boff + cb + 1) - b0;
       const int nkq = (nz + 3) >> 2, ntask = ny * nkq;
+      if (S == SEMI_VITERBI && J.interleaved && ntask <= 64 && ny <= 32 && nz <= 32) {
+        // outer product with each split's member values staged in shared
+        // memory: per step a lane loads one A and one B member of two live
+        // splits, then every task reads its operands from the stage
+        float(*st)[2][32] = reinterpret_cast<float(*)[2][32]>(sm.stage + warp * 128);
+        const int my_a = lane < ny ? __ldg(amem + a0 + lane) : -1;
+        const int my_b = lane < nz ? __ldg(bmem + b0 + lane) : -1;
+        int tj[2], tk[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const int t = lane + 32 * u;
+          tj[u] = t < ntask ? t / nkq : -1;
+          tk[u] = t < ntask ? (t - tj[u] * nkq) * 4 : 0;
+        }
+        float acc[2][4];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[u][q] = -CUDART_INF_F;
+        for (unsigned long long mm = m; mm;) {
+          const int s0 = __ffsll(mm) - 1;
+          mm &= mm - 1;
+          const int s1 = mm ? __ffsll(mm) - 1 : s0;
+          if (mm) mm &= mm - 1;
+          st[0][0][lane] = my_a >= 0 ? __ldg(X.aptr[c0 + s0] + my_a) : -CUDART_INF_F;
+          st[0][1][lane] = my_b >= 0 ? __ldg(X.bptr[c0 + s0] + my_b) : -CUDART_INF_F;
+          st[1][0][lane] = my_a >= 0 ? __ldg(X.aptr[c0 + s1] + my_a) : -CUDART_INF_F;
+          st[1][1][lane] = my_b >= 0 ? __ldg(X.bptr[c0 + s1] + my_b) : -CUDART_INF_F;
+          __syncwarp();
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            if (tj[u] < 0) continue;
+            const float x0 = st[0][0][tj[u]], x1 = st[1][0][tj[u]];
+            const float4 y0 = *reinterpret_cast<const float4*>(&st[0][1][tk[u]]);
+            const float4 y1 = *reinterpret_cast<const float4*>(&st[1][1][tk[u]]);
+            acc[u][0] = fmaxf(acc[u][0], fmaxf(x0 + y0.x, x1 + y1.x));
+            acc[u][1] = fmaxf(acc[u][1], fmaxf(x0 + y0.y, x1 + y1.y));
+            acc[u][2] = fmaxf(acc[u][2], fmaxf(x0 + y0.z, x1 + y1.z));
+            acc[u][3] = fmaxf(acc[u][3], fmaxf(x0 + y0.w, x1 + y1.w));
+          }
+          __syncwarp();
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          if (tj[u] < 0) continue;
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            if (tk[u] + q < nz) Mw[tj[u] * nz + tk[u] + q] = acc[u][q];
+        }
+      } else
       // outer product over the live splits: M[j][k] = max_s A_s[Y_j] + B_s[Z_k]
       for (int t = lane; t < ntask; t += 32) {
         const int j = t / nkq, k0 = (t - j * nkq) * 4;
@@ -773,7 +826,7 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 size_t pass_smem_bytes(const DevLevel& L, int chunk) {
   const size_t cs = L.cell_size;
   if (L.mode == 2)
-    return (2 * cs + (size_t)(kThreads / 32) * L.max_mtile) * sizeof(float) +
+    return (2 * cs + (size_t)(kThreads / 32) * (128 + L.max_mtile)) * sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int);
   return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);
 }
