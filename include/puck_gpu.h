@@ -58,9 +58,10 @@ typedef struct puck_options {
   int32_t max_batch_sentences;/* cap on sentences per batch (0: no cap beyond memory) */
   float prune_threshold;      /* coarse-pass log max-marginal threshold (reference: -9, CLParser.scala:226) */
   int32_t use_graphs;         /* non-zero: capture each batch's pass sequence in a CUDA graph */
-  int32_t tensor_cores;       /* non-zero: the sum-product fine level's inside binary sums run on
-                                 tcgen05 tensor cores in BF16 with FP32 accumulation (levels whose
-                                 structure the form does not cover keep the FP32 path) */
+  int32_t tensor_cores;       /* non-zero: in puck_parse / puck_partitions / puck_inside_outside the
+                                 sum-product fine level's inside binary sums run on tcgen05 tensor
+                                 cores in BF16 with FP32 accumulation (levels whose structure the
+                                 form does not cover, and the server, keep the FP32 path) */
 } puck_options;
 
 /* One node of a preorder tree (the reference's tree_t, CLViterbi.scala:378):
