@@ -276,8 +276,14 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         // memory: per step a lane loads one A and one B member of two live
         // splits, then every task reads its operands from the stage
         float(*st)[2][32] = reinterpret_cast<float(*)[2][32]>(sm.stage + warp * 128);
+        // ny, nz <= 16: one load per lane stages both operands (lanes 0-15 the
+        // A members, lanes 16-31 the B members) into st[s][0]
+        const bool narrow = ny <= 16 && nz <= 16;
         const int my_a = lane < ny ? __ldg(amem + a0 + lane) : -1;
         const int my_b = lane < nz ? __ldg(bmem + b0 + lane) : -1;
+        const int my_n = lane < 16 ? (lane < ny ? __ldg(amem + a0 + lane) : -1)
+                                   : (lane - 16 < nz ? __ldg(bmem + b0 + lane - 16) : -1);
+        const int yoff = narrow ? 16 : 0;
         int tj[2], tk[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
@@ -295,17 +301,24 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
           mm &= mm - 1;
           const int s1 = mm ? __ffsll(mm) - 1 : s0;
           if (mm) mm &= mm - 1;
-          st[0][0][lane] = my_a >= 0 ? __ldg(X.aptr[c0 + s0] + my_a) : -CUDART_INF_F;
-          st[0][1][lane] = my_b >= 0 ? __ldg(X.bptr[c0 + s0] + my_b) : -CUDART_INF_F;
-          st[1][0][lane] = my_a >= 0 ? __ldg(X.aptr[c0 + s1] + my_a) : -CUDART_INF_F;
-          st[1][1][lane] = my_b >= 0 ? __ldg(X.bptr[c0 + s1] + my_b) : -CUDART_INF_F;
+          if (narrow) {
+            const float* r0 = lane < 16 ? X.aptr[c0 + s0] : X.bptr[c0 + s0];
+            const float* r1 = lane < 16 ? X.aptr[c0 + s1] : X.bptr[c0 + s1];
+            st[0][0][lane] = my_n >= 0 ? __ldg(r0 + my_n) : -CUDART_INF_F;
+            st[1][0][lane] = my_n >= 0 ? __ldg(r1 + my_n) : -CUDART_INF_F;
+          } else {
+            st[0][0][lane] = my_a >= 0 ? __ldg(X.aptr[c0 + s0] + my_a) : -CUDART_INF_F;
+            st[0][1][lane] = my_b >= 0 ? __ldg(X.bptr[c0 + s0] + my_b) : -CUDART_INF_F;
+            st[1][0][lane] = my_a >= 0 ? __ldg(X.aptr[c0 + s1] + my_a) : -CUDART_INF_F;
+            st[1][1][lane] = my_b >= 0 ? __ldg(X.bptr[c0 + s1] + my_b) : -CUDART_INF_F;
+          }
           __syncwarp();
 #pragma unroll
           for (int u = 0; u < 2; ++u) {
             if (tj[u] < 0) continue;
             const float x0 = st[0][0][tj[u]], x1 = st[1][0][tj[u]];
-            const float4 y0 = *reinterpret_cast<const float4*>(&st[0][1][tk[u]]);
-            const float4 y1 = *reinterpret_cast<const float4*>(&st[1][1][tk[u]]);
+            const float4 y0 = *reinterpret_cast<const float4*>(&st[0][narrow ? 0 : 1][yoff + tk[u]]);
+            const float4 y1 = *reinterpret_cast<const float4*>(&st[1][narrow ? 0 : 1][yoff + tk[u]]);
             acc[u][0] = fmaxf(acc[u][0], fmaxf(x0 + y0.x, x1 + y1.x));
             acc[u][1] = fmaxf(acc[u][1], fmaxf(x0 + y0.y, x1 + y1.y));
             acc[u][2] = fmaxf(acc[u][2], fmaxf(x0 + y0.z, x1 + y1.z));
