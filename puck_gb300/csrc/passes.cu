@@ -54,6 +54,7 @@ struct CellCtx {
   int g, G;   // this CTA is part g of the cell's G parts
   int last;
   int wcnt[kThreads / 32];
+  unsigned segpass[kMaxSeg / 32];  // bit s: segment s of the current job is gated in for this cell
   unsigned long long work, corner;
 };
 
@@ -203,6 +204,14 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
   float* Mw = sm.M + warp * L.max_mtile;
   const int nsp = X.nsp;
   unsigned long long work = 0, corner = 0;
+  // the cell's gate per segment, one ballot per 32 segments (read after the
+  // first barrier below)
+  for (int base = 0; base < J.nseg; base += blockDim.x) {
+    const int sg = base + threadIdx.x;
+    const bool hit = sg < J.nseg && (!gated || gate_hit(J, sg, ms, L.gate_merged, X.gate));
+    const unsigned b = __ballot_sync(kFull, hit);
+    if (lane == 0 && sg < J.nseg) X.segpass[sg >> 5] = b;
+  }
   for (int c0 = 0; c0 < nsp; c0 += kPairChunk) {
     const int nc = min(kPairChunk, nsp - c0);
     for (int i = threadIdx.x; i < nc * ms; i += blockDim.x) {
@@ -394,7 +403,10 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       // every rule of the pair's gated-in blocks: M[j][k] (x) w into its target
       const int bk1 = __ldg(J.pair_blk + p + 1);
       for (int bk = __ldg(J.pair_blk + p); bk < bk1; ++bk) {
-        if (gated && !gate_hit(J, __ldg(J.blk_seg + bk), ms, L.gate_merged, X.gate)) continue;
+        {
+          const int sg = __ldg(J.blk_seg + bk);
+          if (!((X.segpass[sg >> 5] >> (sg & 31)) & 1u)) continue;
+        }
         int cur = -1;
         float run = Sr<S>::zero();
         if (!J.interleaved) {

@@ -19,6 +19,7 @@ constexpr int kMaxMask = 8;        // up to 256 coarse symbols
 constexpr int kMaxCoarse = 256;
 constexpr int kMaxSplitChunk = 32;  // splits staged in shared memory at once
 constexpr int kMaxLen = 256;        // longest sentence a parser accepts
+constexpr int kMaxSeg = 2048;       // rule segments of one job (coarse parents x sub-segments)
 
 // A job's rules in CSR over target symbols.  rules[k] = {a | b << 16, bits(w)}
 // with value = (A[a] + B[b]) + w (Viterbi) or A[a] * B[b] * w (Real).

@@ -330,6 +330,7 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.tgt_seg = up<int>(D, L, n + "/tgt_seg", "i4");
     J.seg_bits = up<int>(D, L, n + "/seg_bits", "i4", &nseg);
     J.nseg = (int)(nseg / std::max(1, L.mask_size));
+    if (J.nseg > puck::kMaxSeg) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "more than 2048 rule segments in " + n};
     static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
     static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
     int64_t npk = 0, nr = 0, nbp = 0;
