@@ -100,6 +100,16 @@ __device__ __forceinline__ void atomic_fmax(float* addr, float v) {
 }
 
 template <int S>
+__device__ __forceinline__ void put_split(CellCtx& X, int k, const float* a, const float* b, const int* la,
+                                          const int* lb, float ls, float rs, float ps) {
+  X.aptr[k] = a;
+  X.bptr[k] = b;
+  X.alive[k] = la;
+  X.blive[k] = lb;
+  if (S == SEMI_REAL) X.scl[k] = __expf(-ps + rs + ls);
+}
+
+template <int S>
 __device__ __forceinline__ void add_split(CellCtx& X, const float* a, const float* b, const int* la,
                                           const int* lb, float ls, float rs, float ps) {
   int k = X.nsp++;
@@ -631,13 +641,29 @@ __global__ void __launch_bounds__(256, S == SEMI_REAL && MODE == 2 ? 5 : 6)
       const int jid = job == 0 ? IN_TT : job == 1 ? IN_NT : job == 2 ? IN_TN : IN_NN;
       if (jid == IN_TT && span != 2) continue;
       if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
-      if (threadIdx.x == 0) {
-        X.nsp = 0;
-        if (jid == IN_NT) split(TOP(b, e - 1), BOT(e - 1, e));
-        else if (jid == IN_TN) split(BOT(b, b + 1), TOP(b + 1, e));
-        else if (jid == IN_TT) split(BOT(b, b + 1), BOT(b + 1, e));
-        else
-          for (int sp = b + 1; sp < e; ++sp) split(TOP(b, sp), TOP(sp, e));
+      if (jid != IN_NN) {
+        if (threadIdx.x == 0) {
+          X.nsp = 0;
+          if (jid == IN_NT) split(TOP(b, e - 1), BOT(e - 1, e));
+          else if (jid == IN_TN) split(BOT(b, b + 1), TOP(b + 1, e));
+          else split(BOT(b, b + 1), BOT(b + 1, e));
+        }
+      } else if (threadIdx.x < 32) {
+        // the allowed splits, 32 at a time (their mask loads in parallel),
+        // kept in split order
+        const int lane = threadIdx.x;
+        int k0 = 0;
+        for (int sp0 = b + 1; sp0 < e; sp0 += 32) {
+          const int sp = sp0 + lane;
+          const long long lc = sp < e ? TOP(b, sp) : 0, rc = sp < e ? TOP(sp, e) : 0;
+          const bool ok = sp < e && mask_any(M, lc) && mask_any(M, rc);
+          const unsigned bal = __ballot_sync(kFull, ok);
+          if (ok)
+            put_split<S>(X, k0 + __popc(bal & ((1u << lane) - 1u)), inside + lc * cs, inside + rc * cs,
+                         V.in + lc * ms, V.in + rc * ms, scale_of(M.iscale, lc), scale_of(M.iscale, rc), ps);
+          k0 += __popc(bal);
+        }
+        if (lane == 0) X.nsp = k0;
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
@@ -714,6 +740,32 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
       add_split<S>(X, inside + ic * cs, outside + oc * cs, V.in + ic * ms, V.out + oc * ms, scale_of(IS, ic),
                    scale_of(OS, oc), ps);
   };
+  // the allowed splits sp in [lo, hi) of a range job, built by warp 0 32 at a
+  // time (mask loads in parallel) in split order; cells(sp, c1, c2) names the
+  // operand cells, outside-then-inside when oi
+  auto range_splits = [&](int lo, int hi, bool oi, auto cells) {
+    if (threadIdx.x >= 32) return;
+    const int lane = threadIdx.x;
+    int k0 = 0;
+    for (int s0 = lo; s0 < hi; s0 += 32) {
+      const int sp = s0 + lane;
+      long long c1 = 0, c2 = 0;
+      if (sp < hi) cells(sp, c1, c2);
+      const bool ok = sp < hi && mask_any(M, c1) && mask_any(M, c2);
+      const unsigned bal = __ballot_sync(kFull, ok);
+      if (ok) {
+        const int k = k0 + __popc(bal & ((1u << lane) - 1u));
+        if (oi)
+          put_split<S>(X, k, outside + c1 * cs, inside + c2 * cs, V.out + c1 * ms, V.in + c2 * ms, scale_of(OS, c1),
+                       scale_of(IS, c2), ps);
+        else
+          put_split<S>(X, k, inside + c1 * cs, outside + c2 * cs, V.in + c1 * ms, V.out + c2 * ms, scale_of(IS, c1),
+                       scale_of(OS, c2), ps);
+      }
+      k0 += __popc(bal);
+    }
+    if (lane == 0) X.nsp = k0;
+  };
   if (span == n) {
     if (threadIdx.x == 0) P[L.root] = Sr<S>::one();  // setRootScores
   } else if (X.flag0) {
@@ -721,16 +773,22 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
     for (int job = 0; job < 4; ++job) {
       const int jid = job == 0 ? OUT_R_TN : job == 1 ? OUT_L_NT : job == 2 ? OUT_L_NN : OUT_R_NN;
       if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
-      if (threadIdx.x == 0) {
+      if (jid == OUT_L_NN) {
+        range_splits(e + 1, n + 1, true, [&](int sp, long long& c1, long long& c2) {
+          c1 = BOT(b, sp);
+          c2 = TOP(e, sp);
+        });
+      } else if (jid == OUT_R_NN) {
+        range_splits(0, b, false, [&](int sp, long long& c1, long long& c2) {
+          c1 = TOP(sp, b);
+          c2 = BOT(sp, e);
+        });
+      } else if (threadIdx.x == 0) {
         X.nsp = 0;
         if (jid == OUT_R_TN) {
           if (b >= 1) split_io(BOT(b - 1, b), BOT(b - 1, e));
-        } else if (jid == OUT_L_NT) {
-          if (e + 1 <= n) split_oi(BOT(b, e + 1), BOT(e, e + 1));
-        } else if (jid == OUT_L_NN) {
-          for (int sp = e + 1; sp <= n; ++sp) split_oi(BOT(b, sp), TOP(e, sp));
-        } else {
-          for (int sp = 0; sp < b; ++sp) split_io(TOP(sp, b), BOT(sp, e));
+        } else if (e + 1 <= n) {
+          split_oi(BOT(b, e + 1), BOT(e, e + 1));
         }
       }
       __syncthreads();
@@ -759,16 +817,22 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
     for (int job = 0; job < 4; ++job) {
       const int jid = job == 0 ? OUT_L_TT : job == 1 ? OUT_R_NT : job == 2 ? OUT_L_TN : OUT_R_TT;
       if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
-      if (threadIdx.x == 0) {
+      if (jid == OUT_R_NT) {
+        range_splits(0, b, false, [&](int sp, long long& c1, long long& c2) {
+          c1 = TOP(sp, b);
+          c2 = BOT(sp, b + 1);
+        });
+      } else if (jid == OUT_L_TN) {
+        range_splits(b + 2, n + 1, true, [&](int sp, long long& c1, long long& c2) {
+          c1 = BOT(b, sp);
+          c2 = TOP(b + 1, sp);
+        });
+      } else if (threadIdx.x == 0) {
         X.nsp = 0;
         if (jid == OUT_L_TT) {
           if (b + 2 <= n) split_oi(BOT(b, b + 2), BOT(b + 1, b + 2));
-        } else if (jid == OUT_R_NT) {
-          for (int sp = 0; sp < b; ++sp) split_io(TOP(sp, b), BOT(sp, b + 1));
-        } else if (jid == OUT_L_TN) {
-          for (int sp = b + 2; sp <= n; ++sp) split_oi(BOT(b, sp), TOP(b + 1, sp));
-        } else {
-          if (b >= 1) split_io(BOT(b - 1, b), BOT(b - 1, b + 1));
+        } else if (b >= 1) {
+          split_io(BOT(b - 1, b), BOT(b - 1, b + 1));
         }
       }
       __syncthreads();
