@@ -71,7 +71,8 @@ struct Smem {
   int* list;
 };
 
-__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk) {
+// with_stage: the per-warp operand stage of the Viterbi inside pass
+__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage) {
   Smem m;
   const int cs = L.cell_size;
   m.P = base;
@@ -81,8 +82,10 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk)
   m.pl = nullptr;
   m.list = nullptr;
   if (L.mode == 2) {
-    m.stage = rest;
-    rest += (blockDim.x >> 5) * 128;
+    if (with_stage) {
+      m.stage = rest;
+      rest += (blockDim.x >> 5) * 128;
+    }
     m.M = rest;
     m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * L.max_mtile);
     m.list = reinterpret_cast<int*>(m.pl + L.n_coarse * L.mask_size);
@@ -601,7 +604,7 @@ __global__ void __launch_bounds__(256, S == SEMI_REAL && MODE == 2 ? 5 : 6)
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk);
+  const Smem sm = carve(smem, L, chunk, S == SEMI_VITERBI);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -698,7 +701,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk);
+  const Smem sm = carve(smem, L, chunk, false);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -912,10 +915,10 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
-size_t pass_smem_bytes(const DevLevel& L, int chunk) {
+size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage) {
   const size_t cs = L.cell_size;
   if (L.mode == 2)
-    return (2 * cs + (size_t)(kThreads / 32) * (128 + L.max_mtile)) * sizeof(float) +
+    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? 128 : 0) + L.max_mtile)) * sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int);
   return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);
 }
@@ -952,7 +955,7 @@ cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, 
                         int max_span, const float* inside_c, float* inside, float* outside, DevLive V, Counters C,
                         cudaStream_t st) {
   const int chunk = pick_split_chunk(L.cell_size, max_span);
-  const size_t smem = pass_smem_bytes(L, chunk);
+  const size_t smem = pass_smem_bytes(L, chunk, inside_pass && S == SEMI_VITERBI);
   const unsigned grid = (unsigned)W.nunits;
   if (inside_pass) {
     if (cudaError_t e = set_smem(k_inside_span<S, MODE>, smem); e != cudaSuccess) return e;

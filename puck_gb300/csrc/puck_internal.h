@@ -191,7 +191,7 @@ cudaError_t launch_mbr_decode(const DevBatch& B, const DevWork& W, const DevMask
 cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
                                const float* inside, const double* part_scale, float* log_z, cudaStream_t st);
 
-size_t pass_smem_bytes(const DevLevel& L, int chunk);
+size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage);
 
 // Tensor-core inside pass: the binary sums of the cells of one span.  cells
 // holds (sentence, begin) pairs; 128 cells per tile, one CTA per tile and
