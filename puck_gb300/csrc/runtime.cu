@@ -1294,7 +1294,10 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
       P->levels.emplace_back(new LevelDev());
       LevelDev& LD = *P->levels.back();
       build_level(LD, g->levels[l], l < nl - 1 && nl != 1);
-      if (P->opt.tensor_cores && l == nl - 1) LD.tc_ok = build_tc(LD, g->levels[l], &LD.tc_why);
+      if (P->opt.tensor_cores) {
+        if (l == nl - 1) LD.tc_ok = build_tc(LD, g->levels[l], &LD.tc_why);
+        else LD.tc_why = "a coarse level of the cascade (it only makes masks)";
+      }
     }
     P->bufs.resize(nl);
     size_t free_b = 0, total_b = 0;

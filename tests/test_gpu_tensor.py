@@ -113,3 +113,22 @@ def test_tc_mbr_trees_close_to_fp32_path():
         same += np.array_equal(nt[o:o + k, :3], nf[o:o + k, :3])
         o += k
     assert same >= 0.9 * len(lens), (same, len(lens))
+
+
+def test_tensor_cores_option_on_a_viterbi_level_keeps_the_fp32_path():
+    """tensor_cores on a Viterbi cascade: the level reports why the form does
+    not apply, and the parse is the oracle's, bit for bit."""
+    import oracle
+    from helpers import split_levels, split_sentences, write_grz
+    from puck_gb300.parser import CLParser, pack_sentences
+    levels = split_levels("viterbi", "small")
+    sents = split_sentences(16, seed=65, n_words=300, mean=12, hi=30)
+    words, offsets, _ = pack_sentences(sents)
+    P = CLParser(write_grz(levels, "split_small"), max_alloc_size=2 << 30, tensor_cores=True)
+    on, why = P.tensor_cores(len(levels) - 1)
+    assert not on and "sum-product" in why
+    on0, why0 = P.tensor_cores(0)  # only the parsing level is considered
+    assert not on0 and "coarse level" in why0
+    nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all()
+    assert np.array_equal(nodes, oracle.run(levels, sents, mode="parse").trees())
