@@ -35,6 +35,11 @@ def split_levels(fine_semiring="viterbi", size="medium"):
         # many coarse pairs per job (hundreds of live pairs per cell), small splits
         c, f = synth.split_grammar(seed=6, n_coarse_nt=30, n_coarse_pt=20, max_split=4, mean_split=3.0,
                                    n_coarse_rules=1500, target_fine_rules=40000, n_coarse_unaries=40, n_words=400)
+    elif size == "deep":
+        # coarse symbols with up to 30 refinements: outer-product tiles on
+        # each path of the fine kernel (<= 16 members, <= 32, and larger tiles)
+        c, f = synth.split_grammar(seed=11, n_coarse_nt=8, n_coarse_pt=6, max_split=30, mean_split=13.0,
+                                   n_coarse_rules=70, target_fine_rules=30000, n_coarse_unaries=12, n_words=300)
     elif size == "medium":
         c, f = synth.split_grammar(seed=4, n_coarse_nt=10, n_coarse_pt=8, max_split=8, mean_split=6.0,
                                    n_coarse_rules=120, target_fine_rules=20000, n_coarse_unaries=20, n_words=500)

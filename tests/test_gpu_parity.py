@@ -99,6 +99,22 @@ def test_wide_grammar_split_cells_bit_exact():
     assert np.array_equal(nodes, r.trees())
 
 
+def test_deep_refinements_bit_exact():
+    """Coarse symbols with up to 30 refinements: the fine kernel's
+    outer products run on all three of its paths (both operands staged by one
+    load, staged separately, and the unstaged loop for larger tiles)."""
+    levels = split_levels("viterbi", "deep")
+    sents = split_sentences(24, seed=67, n_words=300, mean=16, hi=30)
+    P = gpu(levels, "split_deep")
+    words, offsets, _ = pack_sentences(sents)
+    nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all()
+    r = oracle.run(levels, sents, mode="parse")
+    assert np.array_equal(bits(P.debug_copy(0, "inside")), bits(r.chart(0, "inside")))
+    assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
+    assert np.array_equal(nodes, r.trees())
+
+
 def test_bench_grammar_bit_exact():
     """The 1,091-symbol, 1.5M-rule bench grammar on 40 sentences up to 40
     words: split long cells, hundreds of live pairs, the batched inside form."""
