@@ -111,10 +111,6 @@ struct TcCells {
   uint64_t bar[2], bar_fin;
 };
 
-__device__ __forceinline__ bool live_bit(const int* live, long long cell, int ms, int c) {
-  return (__ldg(live + cell * ms + (c >> 5)) >> (c & 31)) & 1;
-}
-
 // Operand cells of split i of cell r for a job; false if the split is out of
 // range or not allowed (an operand cell pruned).
 __device__ __forceinline__ bool split_cells(const TcCells& X, const DevBatch& B, int r, int job, int span, int i,
