@@ -150,7 +150,48 @@ def cpu_baseline(levels, sents, sample: int):
     return {"value": round(len(sub) / dt, 3), "unit": "sentences/s", "cores": threads, "kind": "port",
             "sample": f"first {len(sub)} sentences of the workload (mean length "
                       f"{np.mean([len(s) for s in sub]):.1f}), full cascade: coarse inside/outside, masks, "
-                      f"fine inside, backtrace; {dt:.1f}s"}
+                      f"fine inside, backtrace; {dt:.1f}s"}, r
+
+
+def parity(path, sents, batch_nodes, r, device: int):
+    """The GPU's results on the CPU-baseline sample against the oracle's
+    (the oracle run ``r`` of that sample): the sample's trees taken from the
+    timed full-workload batch, and the sample parsed again as its own batch
+    for its pruning masks and charts.  Viterbi results must be bit-identical;
+    a tree that differs counts as explained only when its root score is
+    within 1e-5 relative of the oracle's (a near-tie)."""
+    import numpy as np
+    from puck_gb300.parser import CLParser, pack_sentences
+    sub = sents[:len(r.lengths)]
+    lens = [len(s) for s in sub]
+    k = sum(2 * n - 1 for n in lens)
+    ref = r.trees()
+    got = batch_nodes[:k]
+    same, near, start = 0, 0, 0
+    for n in lens:
+        a, b = got[start:start + 2 * n - 1], ref[start:start + 2 * n - 1]
+        start += 2 * n - 1
+        if np.array_equal(a, b):
+            same += 1
+        else:
+            sa, sb = float(a[0, 3:4].view(np.float32)[0]), float(b[0, 3:4].view(np.float32)[0])
+            near += abs(sa - sb) <= 1e-5 * abs(sb)
+    P = CLParser(path, max_alloc_size=8 << 30, device=device, max_length=MAX_LEN)
+    w, o, _ = pack_sentences(sub)
+    alone, st = P.parse_ids(w, o)
+    assert (st == 0).all()
+    bits = lambda x: np.ascontiguousarray(x).view(np.int32)
+    masks_same = bool(np.array_equal(P.debug_copy(0, "masks"), r.masks(0)[0]))
+    coarse_same = bool(np.array_equal(bits(P.debug_copy(0, "inside")), bits(r.chart(0, "inside"))) and
+                       np.array_equal(bits(P.debug_copy(0, "outside")), bits(r.chart(0, "outside"))))
+    fine_same = bool(np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside"))))
+    P.release()
+    return {"sentences": len(sub), "trees_identical": same, "masks_identical": masks_same,
+            "coarse_charts_identical": coarse_same, "fine_inside_chart_identical": fine_same,
+            "alone_equals_batch": bool(np.array_equal(alone, got)),
+            "divergences_within_1e-5": int(near), "divergences_unexplained": int(len(sub) - same - near),
+            "oracle_corner_drops": int(r.corner_drops(1)),
+            "note": "oracle = CPU restatement of the reference's cascade; trees from the timed batch"}
 
 
 def plain_baseline(path, sents, sample: int, device: int):
@@ -337,9 +378,8 @@ def run_ours(args):
     avg_launch_s = fine_in_ms / 1e3 / max(fine_in_launch, 1)
     achieved = per_launch_ops / avg_launch_s / 1e12
     # DRAM traffic per work unit of the fine inside kernel, measured with ncu
-    # over all fine inside launches of a 2,000-sentence run of this workload
-    # (profiles/traffic_k_inside_span_split_viterbi_2000.md), scaled to this
-    # run's average launch
+    # on fine inside launches of a 2,000-sentence run of this workload, scaled
+    # to this run's average launch
     traffic = FINE_INSIDE_BYTES_PER_UNIT * work / max(fine_in_launch, 1)
     out = {
         "metric": "sentences/sec, 1.1k-symbol grammar, len<=40 (batched/served vs plain); p50/p99 ms",
@@ -373,7 +413,9 @@ def run_ours(args):
     P.release()
     if rank == 0 and world == 1:
         if args.cpu_sample > 0:
-            out["cpu_baseline"] = cpu_baseline(levels, sents, args.cpu_sample)
+            out["cpu_baseline"], r_cpu = cpu_baseline(levels, sents, args.cpu_sample)
+            out["parity"] = parity(path, sents, nodes, r_cpu, local)
+            log(f"parity: {out['parity']}")
         if args.plain_sample > 0:
             out["plain"] = plain_baseline(path, sents, args.plain_sample, local)
             out["plain"]["batched_over_plain"] = round(value / out["plain"]["value"], 2)

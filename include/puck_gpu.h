@@ -83,7 +83,9 @@ typedef struct puck_tree_node {
  * ms_decode per pass kind over all levels. */
 typedef struct puck_stats {
   double ms_total, ms_inside, ms_outside, ms_masks, ms_decode, ms_h2d, ms_d2h;
-  int64_t cells, cells_pruned, batches, kernel_launches;
+  int64_t cells;              /* chart cells (bot + top halves) of the batches */
+  int64_t cells_pruned;       /* of those, cells the last coarse level's mask closes entirely */
+  int64_t batches, kernel_launches;
   int64_t binary_work;        /* (rule, split) applications executed in the last call */
   double ms_device;
   int64_t h2d_bytes, d2h_bytes;
@@ -160,21 +162,26 @@ puck_status puck_parser_level_work(const puck_parser* p, int32_t level, int64_t 
 
 /* Max-constituent (MBR) tree decode into caller-owned device buffers with no
  * device allocation, for callers that cannot allocate at the point where they
- * decode: a host running inside a device arena its own pool carved out, a
- * serving loop that must keep the CUDA allocator off its request path, or
- * work issued while another framework captures the stream.  No counterpart in
- * the reference (its MBR decode runs on the host, CLParser.scala:589-696).
- * Same decode as puck_parse's MBR path: cell_decode (device) holds per cell
- * {best coarse marginal, coarse symbol as int bits} -- the layout
- * puck_debug_copy(which = 5) returns; iscale/oscale (device, per cell) are the
- * coarse level's log-scales for a Real fine level, or both NULL; lengths is a
- * host array; nodes (device) receives sum(2*len_i - 1) preorder nodes.  Work
- * is enqueued on `stream` (a cudaStream_t, NULL = default stream).  Scratch
- * lives in a fixed array in the library's device memory: at most 65,536
- * sentences and sum of 3*(len_i+1)^2 <= 4,194,304 floats per call (larger
- * calls are rejected with PUCK_ERR_INVALID_ARG); the first call on a device
- * resolves the array's address and should precede any stream capture; calls
- * whose work overlaps on the GPU race on the array. */
+ * decode: a host running inside a device arena its own pool carved out (the
+ * pool already owns the device's memory), or a serving loop that must keep
+ * the CUDA allocator off its request path (a cudaMalloc can synchronize the
+ * device).  No counterpart in the reference (its MBR decode runs on the host,
+ * CLParser.scala:589-696).
+ * Same decode as puck_parse's MBR path: cell_decode (device, 8-byte aligned)
+ * holds per cell {best coarse marginal, coarse symbol as int bits} -- the
+ * layout puck_debug_copy(which = 5) returns; iscale/oscale (device, per cell)
+ * are the coarse level's log-scales for a Real fine level, or both NULL;
+ * lengths is a host array; nodes (device) receives
+ * sum(2*len_i - 1) preorder nodes.  Work is enqueued on `stream` (a
+ * cudaStream_t, NULL = default stream).  Scratch lives in a fixed array in
+ * the library's device memory, held by every device that loads the library
+ * until the process exits: at most 65,536 sentences and sum of
+ * 3*(len_i+1)^2 <= 4,194,304 floats (16 MiB) per call; larger calls are
+ * rejected with PUCK_ERR_INVALID_ARG.  The first call on a device resolves
+ * the array's address (cudaGetSymbolAddress, with that device current) and
+ * should come before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU (other streams, other host threads) race on
+ * it and must be serialized by the caller. */
 puck_status puck_mbr_decode_static(const float* cell_decode, const float* iscale, const float* oscale,
                                    const int32_t* lengths, int32_t nsent, puck_tree_node* nodes, void* stream);
 

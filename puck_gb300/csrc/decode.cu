@@ -17,6 +17,13 @@ namespace {
 
 using namespace dev;
 
+// Adds a block's count of fully pruned cells to the launch counter (every
+// thread of the block calls this once).
+__device__ __forceinline__ void flush_pruned(unsigned& block_pruned, unsigned long long* pruned) {
+  __syncthreads();
+  if (threadIdx.x == 0 && pruned && block_pruned) atomicAdd(pruned, (unsigned long long)block_pruned);
+}
+
 // ---------------------------------------------------------------------------
 // Pruning masks: one warp per cell (max-marginal test against root + thresh).
 // Cell c of sentence s (unit i of a per-cell work list).
@@ -33,10 +40,16 @@ __device__ __forceinline__ CellRef cell_ref(const DevBatch& B, const DevWork& W,
 }
 
 __global__ void k_masks(DevLevel L, DevBatch B, DevWork W, const float* inside, const float* outside, float thresh,
-                        int* out) {
+                        int* out, unsigned long long* pruned) {
+  __shared__ unsigned block_pruned;
+  if (threadIdx.x == 0) block_pruned = 0;
+  __syncthreads();
   const long long unit = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (unit >= W.nunits) return;
+  if (unit >= W.nunits) {
+    flush_pruned(block_pruned, pruned);
+    return;
+  }
   const CellRef R = cell_ref(B, W, (int)unit);
   const int s = R.s;
   const long long c = R.c, first = R.first, last = R.last;
@@ -56,11 +69,15 @@ __global__ void k_masks(DevLevel L, DevBatch B, DevWork W, const float* inside, 
         if ((f >> 5) == i) words[i] |= 1u << (f & 31);
     }
   }
+  unsigned any = 0u;
 #pragma unroll
   for (int i = 0; i < kMaxMask; ++i) {
     const unsigned v = __reduce_or_sync(kFull, words[i]);
+    any |= v;
     if (lane == 0 && i < L.mask_size) out[c * L.mask_size + i] = (int)v;
   }
+  if (lane == 0 && !any) atomicAdd(&block_pruned, 1u);  // no coarse symbol survives: the next level skips the cell
+  flush_pruned(block_pruned, pruned);
 }
 
 // Per-cell log-scale: max over the cell, -9000 floor mapped to 0.
@@ -281,10 +298,11 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 }  // namespace
 
 cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const DevWork& W, const float* inside,
-                         const float* outside, float thresh, int* masks_out, cudaStream_t st) {
+                         const float* outside, float thresh, int* masks_out, cudaStream_t st,
+                         unsigned long long* pruned) {
   const int blocks = (int)((W.nunits * 32 + 255) / 256);
   if (blocks == 0) return cudaSuccess;
-  k_masks<<<blocks, 256, 0, st>>>(L, B, W, inside, outside, thresh, masks_out);
+  k_masks<<<blocks, 256, 0, st>>>(L, B, W, inside, outside, thresh, masks_out, pruned);
   return cudaGetLastError();
 }
 

@@ -3,10 +3,9 @@
 //
 // Some callers cannot allocate device memory at the point where they decode:
 // a JVM host that runs the parser inside a device arena its own pool carved
-// out up front, a serving loop whose request path must never enter the CUDA
-// allocator (a cudaMalloc can synchronize the device and stall every stream),
-// or code that issues work while another framework is capturing the stream
-// into a CUDA graph, where cudaMalloc is not permitted.  puck_parse's MBR path
+// out up front (every byte of the device already belongs to that pool), or a
+// serving loop whose request path must never enter the CUDA allocator (a
+// cudaMalloc can synchronize the device and stall every stream).  puck_parse's MBR path
 // allocates its dynamic-programming tables with the rest of its batch
 // buffers; this entry point runs the same per-sentence decode
 // (mbr_decode_sentence) but keeps that scratch -- the sentences' lengths and
@@ -26,6 +25,7 @@
 #include "../../include/puck_gpu.h"
 
 #include <cstddef>
+#include <cstdint>
 #include <mutex>
 #include <string>
 
@@ -106,6 +106,11 @@ extern "C" puck_status puck_mbr_decode_static(const float* cell_decode, const fl
     return fail(PUCK_ERR_INVALID_ARG, "puck_mbr_decode_static: null argument or negative sentence count");
   if ((iscale == nullptr) != (oscale == nullptr))
     return fail(PUCK_ERR_INVALID_ARG, "puck_mbr_decode_static: give both scale arrays or neither");
+  // the kernels read cell_decode as {score, symbol} pairs (8-byte loads)
+  auto misaligned = [](const void* p, uintptr_t a) { return reinterpret_cast<uintptr_t>(p) % a != 0; };
+  if (misaligned(cell_decode, 8) || misaligned(nodes, 4) || misaligned(iscale, 4) || misaligned(oscale, 4))
+    return fail(PUCK_ERR_INVALID_ARG,
+                "puck_mbr_decode_static: cell_decode must be 8-byte aligned, nodes and scales 4-byte aligned");
   if (nsent > kStaticMaxSentences)
     return fail(PUCK_ERR_INVALID_ARG, "puck_mbr_decode_static: more than " + std::to_string(kStaticMaxSentences) +
                                           " sentences in one call");

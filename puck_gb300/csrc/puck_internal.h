@@ -177,8 +177,10 @@ cudaError_t launch_inside_span(const DevLevel& L, const DevBatch& B, const DevWo
 cudaError_t launch_outside_span(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
                                 int max_span, const float* inside, float* outside, DevLive V, Counters C,
                                 cudaStream_t st);
+// pruned (may be null) counts the cells whose mask has no bit set
 cudaError_t launch_masks(const DevLevel& L, const DevBatch& B, const DevWork& W, const float* inside,
-                         const float* outside, float thresh, int* masks_out, cudaStream_t st);
+                         const float* outside, float thresh, int* masks_out, cudaStream_t st,
+                         unsigned long long* pruned = nullptr);
 cudaError_t launch_scaling(int cell_size, const DevBatch& B, const DevWork& W, const float* chart, float* out,
                            cudaStream_t st);
 cudaError_t launch_viterbi(const DevLevel& L, const DevBatch& B, const DevWork& W, int max_len, const float* inside,

@@ -943,8 +943,9 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   Wsent.nunits = ns;
   P->b_status.ensure(ns * sizeof(int) + 16);
   CUDA_TRY(cudaMemsetAsync(P->b_status.p, 0, ns * sizeof(int), st));
-  // per level: binary partials >= +0.0 written, (rule, split) work units
-  const size_t ctr_bytes = 2 * nl * sizeof(unsigned long long);
+  // per level: binary partials >= +0.0 written, (rule, split) work units;
+  // then the cells the last coarse level prunes entirely
+  const size_t ctr_bytes = (2 * nl + 1) * sizeof(unsigned long long);
   P->b_counters.ensure(ctr_bytes);
   CUDA_TRY(cudaMemsetAsync(P->b_counters.p, 0, ctr_bytes, st));
   if (part_units > 0) {
@@ -1016,7 +1017,8 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     rec(EV[2]);
     if (!last) {
       lb.masks.ensure(num_cells * D.mask_size * sizeof(int));
-      CUDA_TRY(puck::launch_masks(D, B, Wcell, inside, outside, P->opt.prune_threshold, lb.masks.as<int>(), st));
+      CUDA_TRY(puck::launch_masks(D, B, Wcell, inside, outside, P->opt.prune_threshold, lb.masks.as<int>(), st,
+                                  l == nl - 2 ? P->b_counters.as<unsigned long long>() + 2 * nl : nullptr));
       ++LC[2];
       lb.iscale.ensure(num_cells * sizeof(float));
       lb.oscale.ensure(num_cells * sizeof(float));
@@ -1098,7 +1100,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     }
   }
   std::vector<int> status(ns);
-  std::vector<unsigned long long> ctr(2 * nl, 0);
+  std::vector<unsigned long long> ctr(2 * nl + 1, 0);
   CUDA_TRY(cudaMemcpyAsync(status.data(), P->b_status.p, ns * sizeof(int), cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaMemcpyAsync(ctr.data(), P->b_counters.p, ctr_bytes, cudaMemcpyDeviceToHost, st));
   CUDA_TRY(cudaStreamSynchronize(st));
@@ -1127,6 +1129,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
   }
   P->stats.ms_device += ms_between(P->ev_batch[0], P->ev_batch[1]);
   P->stats.cells += num_cells;
+  P->stats.cells_pruned += (int64_t)ctr[2 * nl];
   for (int l = 0; l < nl; ++l) {
     P->stats.binary_work += (int64_t)ctr[2 * l + 1];
     P->level_work[l][0] += (int64_t)ctr[2 * l + 1];
@@ -1194,7 +1197,6 @@ puck_status run_call(puck_parser* P, Mode mode, const int32_t* word_ids, const i
     if (!cur.sent.empty()) plans.push_back(std::move(cur));
     for (auto& pl : plans) run_batch(P, mode, pl, word_ids, offsets, nodes_out, node_off, log_z, sent_status);
     P->last_batches = (int)plans.size();
-    P->stats.cells_pruned = 0;
     P->stats.ms_total = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     (void)first_bad;
     return PUCK_OK;

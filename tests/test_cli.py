@@ -17,7 +17,8 @@ import oracle
 from puck_gb300 import berkeley, compile_grammar, grammar, grz, run_parser
 from puck_gb300.parser import CLParserData, Failure, Success, Tree, nodes_to_viterbi_tree
 
-TEXT = "/root/reference/textGrammars"
+# the reference's Berkeley text grammars (dlwh/puck textGrammars/), when a copy is named
+TEXT = os.environ.get("PUCK_TEXT_GRAMMARS", "")
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -103,6 +104,23 @@ def test_berkeley_cascade_parses_english_on_the_oracle(tmp_path):
     assert first.label == "ROOT"
     assert np.isfinite(nodes[0, 3].view(np.float32))
     assert first.preterminal_labels()[-1] == "."
+
+
+def test_wsj_fixture_trees_are_english_parses():
+    """The committed wsj_0 -> wsj_1 fixture (compiled from the reference's
+    text grammars by tests/golden/make_golden.py): its stored trees decode
+    to ROOT trees whose last preterminal is the sentence-final '.'."""
+    d = os.path.join(ROOT, "tests", "golden")
+    data = np.load(os.path.join(d, "wsj01_cascade_viterbi.npz"))
+    lv = CLParserData.read_sequence(os.path.join(d, "wsj01_cascade_viterbi.grz"))[-1]
+    off, trees = data["offsets"], data["trees"]
+    start = 0
+    for i in range(len(off) - 1):
+        n = int(off[i + 1] - off[i])
+        t = nodes_to_viterbi_tree(trees[start:start + 2 * n - 1], lv)
+        start += 2 * n - 1
+        assert t.label == "ROOT" and t.end == n
+        assert t.preterminal_labels()[-1] == "."
 
 
 def _module(mod, *args, **kw):

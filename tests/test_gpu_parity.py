@@ -83,6 +83,10 @@ def test_cascade_masks_charts_trees_bit_exact(size):
     # the masks really prune (otherwise the gating paths are untested)
     pops = np.unpackbits(m.view(np.uint8)).sum() / m.shape[0]
     assert pops < 0.8 * levels[0].n_coarse
+    # cells_pruned counts the cells whose mask has no bit set
+    st = P.stats()
+    assert st["cells"] == m.shape[0]
+    assert st["cells_pruned"] == int((~m.any(axis=1)).sum()) > 0
 
 
 def test_wide_grammar_split_cells_bit_exact():

@@ -82,6 +82,34 @@ def test_server_viterbi_same_alone_and_in_mix_and_oracle():
     assert st["resident_peak"] > 1  # sentences shared the GPU
 
 
+def test_server_lengths_to_60_match_oracle_and_batch():
+    """The serving lengths (lognormal mean 23 clipped 1-60) with several
+    sentences of 41-60 words: each served tree equals the oracle's and the
+    batch parse's, in a mix with short sentences."""
+    levels = split_levels("viterbi", "medium")
+    path = write_grz(levels, "split_medium")
+    sents = split_sentences(36, seed=27, n_words=500, mean=23, hi=60)
+    rng = np.random.default_rng(27)
+    for i, n in zip((3, 11, 19, 30), (45, 52, 58, 60)):
+        sents[i] = rng.integers(0, 500, size=n).astype(np.int32)
+    assert max(len(s) for s in sents) == 60
+    r = oracle.run(levels, sents, mode="parse")
+    ref = node_blocks(r.trees(), [len(s) for s in sents])
+    P = CLParser(path, max_alloc_size=2 << 30)
+    w, o, lens = pack_sentences(sents)
+    nodes, st = P.parse_ids(w, o)
+    assert (st == 0).all()
+    batch = node_blocks(nodes, lens)
+    S = CLServer(path, max_alloc_size=2 << 30, collect=False)
+    try:
+        served = _serve_mix(S, sents, gap_s=0.001, chunk=4)
+    finally:
+        S.close()
+    for i in range(len(sents)):
+        assert np.array_equal(served[i], ref[i]), i
+        assert np.array_equal(batch[i], ref[i]), i
+
+
 def test_server_matches_batch_parse():
     levels = split_levels("viterbi", "small")
     path = write_grz(levels, "split_small")
