@@ -37,11 +37,18 @@ using namespace dev;
 constexpr int kPairChunk = 64;   // splits per liveness chunk (two ballots)
 constexpr int kThreads = 256;
 constexpr int kRuleBatch = 4;   // rules per lane whose loads are in flight together
+// Per-warp operand stage of the Viterbi inside pass: two buffers of 34 rows
+// of four floats (A members 0-15, a -inf row, B members 0-15, a -inf row).
+constexpr int kStageRows = 34;
+constexpr int kStageFloats = 2 * kStageRows * 4;
+constexpr int kStageRowB = 17;
 
 // Shared bookkeeping of one target cell.
-struct CellCtx {
-  const float* aptr[kMaxLen];   // operand cells of each allowed split
-  const float* bptr[kMaxLen];
+struct __align__(16) CellCtx {
+  // operand cells of each allowed split, and four more entries that repeat
+  // the last split (the flat-tile path reads splits in groups of four)
+  const float* aptr[kMaxLen + 4];
+  const float* bptr[kMaxLen + 4];
   const int* alive[kMaxLen];    // their liveness words
   const int* blive[kMaxLen];
   float scl[kMaxLen];           // Real semiring: per-split scale exp(-p + l + r)
@@ -50,6 +57,7 @@ struct CellCtx {
   int gate[kMaxMask];
   unsigned words[kMaxMask];
   int nsp, nlive;
+  int next;   // next live-pair draw of the flat-tile path
   int flag0, flag1;
   int g, G;   // this CTA is part g of the cell's G parts
   int last;
@@ -66,7 +74,7 @@ struct Smem {
   float* stA;
   float* stB;
   float* M;
-  float* stage;  // per warp 128 floats: two splits' staged A and B members (16-byte aligned)
+  float* stage;  // per warp kStageFloats: staged A and B members of four splits (16-byte aligned)
   unsigned* pl;
   int* list;
 };
@@ -84,7 +92,7 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
   if (L.mode == 2) {
     if (with_stage) {
       m.stage = rest;
-      rest += (blockDim.x >> 5) * 128;
+      rest += (blockDim.x >> 5) * kStageFloats;
     }
     m.M = rest;
     m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * L.max_mtile);
@@ -94,6 +102,23 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
     m.stB = rest + chunk * cs;
   }
   return m;
+}
+
+// Two FP32 additions in one instruction (sm_100+ packed f32x2, round to
+// nearest: each lane of the pair is rounded exactly as a scalar add).
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;"
+      : "=l"(r)
+      : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)));
+  return *reinterpret_cast<float2*>(&r);
+}
+
+// max(a, b, c) in one instruction (sm_100+); exact, like fmaxf
+__device__ __forceinline__ float max3(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
 }
 
 // float max through integer atomics (valid for every non-NaN value)
@@ -204,6 +229,152 @@ __device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned lon
   }
 }
 
+// This lane's operand value for each of the four splits of group g (see
+// flat_outer): two 16-byte loads fetch the four row pointers.
+__device__ __forceinline__ float4 load_group(const float* const* rows, int g, unsigned src, bool ok) {
+  const float* p[4];
+  *reinterpret_cast<longlong2*>(&p[0]) = *reinterpret_cast<const longlong2*>(rows + 4 * g);
+  *reinterpret_cast<longlong2*>(&p[2]) = *reinterpret_cast<const longlong2*>(rows + 4 * g + 2);
+  float4 v;
+  v.x = ok ? __ldg(p[0] + src) : -CUDART_INF_F;
+  v.y = ok ? __ldg(p[1] + src) : -CUDART_INF_F;
+  v.z = ok ? __ldg(p[2] + src) : -CUDART_INF_F;
+  v.w = ok ? __ldg(p[3] + src) : -CUDART_INF_F;
+  return v;
+}
+
+// Outer product of one pair in the flat-tile layout (DevJob::pair_desc): lane
+// slot i holds tile entry e = lane + 32 * i = j * nz + k, i < NS, and ends
+// with max over the chunk's splits s of fl(A_s[Y_j] + B_s[Z_k]), which it
+// stores to the warp's M tile.  Splits go in groups of four consecutive
+// allowed splits; a group with no split live for the pair (mask m) is
+// skipped, and a dead split inside a live group adds only -inf terms.  Per
+// group, lanes 0-15 stage the A members of the four splits as one float4 row
+// each, lanes 16-31 the B members; each slot then reads its two rows (one
+// 16-byte load each) and folds four sums into its entry with two packed adds
+// and two 3-input maxes.  The operand loads of the next live group are
+// issued before the current group's arithmetic, into the other of the warp's
+// two stage buffers.  Slots past the tile read the -inf rows and are not
+// stored.
+template <int NS>
+__device__ __forceinline__ void flat_outer(const CellCtx& X, int c0, unsigned long long m, int4 D, float4* st4,
+                                           float* Mw) {
+  const int lane = threadIdx.x & 31;
+  const int ny = D.z & 255, nz = (D.z >> 8) & 255, E = ny * nz;
+  // j = lane / nz, k = lane % nz; then 32 entries further per slot.  The
+  // float quotient is exact here: (lane + 1/2) / nz is at least 1/32 away
+  // from an integer, far beyond the rounding of the product.
+  const float inv = __frcp_rn((float)nz);
+  int j = (int)(((float)lane + 0.5f) * inv), k = lane - j * nz;
+  const int dq = (int)(32.5f * inv), dr = 32 - dq * nz;
+  unsigned off[NS];  // byte offsets of the slot's A row | B row << 16 (buffer 0)
+  float acc[NS];
+#pragma unroll
+  for (int i = 0; i < NS; ++i) {
+    const bool in = lane + 32 * i < E;
+    off[i] = (unsigned)((in ? j : 16) * 16) | (unsigned)((kStageRowB + (in ? k : 16)) * 16) << 16;
+    acc[i] = -CUDART_INF_F;
+    j += dq;
+    k += dr;
+    if (k >= nz) {
+      k -= nz;
+      ++j;
+    }
+  }
+  const bool a_side = lane < 16;
+  const int mem = a_side ? lane : lane - 16;
+  const bool ok = mem < (a_side ? ny : nz);
+  const unsigned src = (a_side ? (unsigned)D.x & 0xffffu : (unsigned)D.x >> 16) + mem;
+  const float* const* rows = (a_side ? X.aptr : X.bptr) + c0;
+  const int my_row = a_side ? mem : kStageRowB + mem;
+  int g = (__ffsll(m) - 1) >> 2;  // first live group (m != 0)
+  float4 v = load_group(rows, g, src, ok);
+  for (int buf = 0;; buf ^= 1) {
+    float4* sb = st4 + buf * kStageRows;
+    sb[my_row] = v;
+    __syncwarp();
+    const unsigned long long rest = g < 15 ? m >> (4 * g + 4) : 0ull;
+    if (rest) {
+      g += 1 + ((__ffsll(rest) - 1) >> 2);
+      v = load_group(rows, g, src, ok);
+    }
+    const char* stb = reinterpret_cast<const char*>(sb);
+#pragma unroll
+    for (int i = 0; i < NS; ++i) {
+      const float4 a = *reinterpret_cast<const float4*>(stb + (off[i] & 0xffffu));
+      const float4 b = *reinterpret_cast<const float4*>(stb + (off[i] >> 16));
+      const float2 t01 = add2(make_float2(a.x, a.y), make_float2(b.x, b.y));
+      const float2 t23 = add2(make_float2(a.z, a.w), make_float2(b.z, b.w));
+      acc[i] = max3(acc[i], t01.x, t01.y);
+      acc[i] = max3(acc[i], t23.x, t23.y);
+    }
+    if (!rest) break;
+  }
+#pragma unroll
+  for (int i = 0; i < NS; ++i)
+    if (lane + 32 * i < E) Mw[lane + 32 * i] = acc[i];
+  __syncwarp();
+}
+
+// The gated-in blocks of one flat-tile pair: each lane runs its one-target
+// slice four rules per record, fl(M[e] + w) folded with packed adds and
+// 3-input maxes, and flushes once per block.  A block's descriptor
+// {segment, first record, end record, rules} is read one block ahead.
+__device__ __forceinline__ void flat_rules(const DevJob& J, const CellCtx& X, int4 D, const float* Mw, float* P,
+                                           unsigned long long& work, unsigned long long& corner) {
+  const int lane = threadIdx.x & 31;
+  const int b0 = D.y, nb = (int)((unsigned)D.z >> 16);
+  int4 nxt = nb > 0 ? __ldg(J.fr_blk + b0) : make_int4(0, 0, 0, 0);
+  for (int q = 0; q < nb; ++q) {
+    const int4 B = nxt;
+    if (q + 1 < nb) nxt = __ldg(J.fr_blk + b0 + q + 1);
+    if (!((X.segpass[B.x >> 5] >> (B.x & 31)) & 1u)) continue;
+    const int t = __ldg(J.fr_tgt + (b0 + q) * 32 + lane);
+    float best = -CUDART_INF_F;
+#pragma unroll 2
+    for (int g = B.y + lane; g < B.z; g += 32) {
+      const unsigned o = __ldg(J.fr_idx + g);
+      const float4 w = __ldg(J.fr_w + g);
+      const float2 t01 = add2(make_float2(Mw[o & 255u], Mw[(o >> 8) & 255u]), make_float2(w.x, w.y));
+      const float2 t23 = add2(make_float2(Mw[(o >> 16) & 255u], Mw[o >> 24]), make_float2(w.z, w.w));
+      best = max3(best, t01.x, t01.y);
+      best = max3(best, t23.x, t23.y);
+    }
+    if (t >= 0) flush_run<SEMI_VITERBI>(P, t, best, corner);
+    if (lane == 0) work += (unsigned long long)B.w;
+  }
+  __syncwarp();
+}
+
+// The live pairs of a flat-tile job for one chunk of splits.  Warps take
+// pairs from a shared counter (this part's pairs are list positions g,
+// g + G, g + 2G, ...), so a warp that drew cheap pairs takes more of them.
+__device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, CellCtx& X, int c0, int nc, int nlive,
+                                           float* Mw, float* P, unsigned long long& work,
+                                           unsigned long long& corner) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float4* st4 = reinterpret_cast<float4*>(sm.stage + warp * kStageFloats);
+  for (;;) {
+    int k = 0;
+    if (lane == 0) k = atomicAdd(&X.next, 1);
+    const int i = X.g + __shfl_sync(kFull, k, 0) * X.G;
+    if (i >= nlive) break;
+    const int p = sm.list[i];
+    const int4 D = __ldg(J.pair_desc + p);
+    const int ca = D.w & 255, cb = (D.w >> 8) & 255;
+    const unsigned lo = __ballot_sync(kFull, lane < nc && bit(X.la[lane], ca) && bit(X.lb[lane], cb));
+    const unsigned hi =
+        __ballot_sync(kFull, lane + 32 < nc && bit(X.la[lane + 32], ca) && bit(X.lb[lane + 32], cb));
+    const unsigned long long m = (unsigned long long)lo | ((unsigned long long)hi << 32);
+    const int E = (D.z & 255) * ((D.z >> 8) & 255);
+    if (E <= 128) flat_outer<4>(X, c0, m, D, st4, Mw);
+    else if (E <= 192) flat_outer<6>(X, c0, m, D, st4, Mw);
+    else flat_outer<8>(X, c0, m, D, st4, Mw);
+    if (lane == 0) work += (unsigned long long)__popcll(m) * E;
+    flat_rules(J, X, D, Mw, P, work, corner);
+  }
+}
+
 // Pair-factored gather (level mode 2), see the file comment.
 template <int S>
 __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
@@ -217,6 +388,16 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
   float* Mw = sm.M + warp * L.max_mtile;
   const int nsp = X.nsp;
   unsigned long long work = 0, corner = 0;
+  if (S == SEMI_VITERBI && J.interleaved == 3 && threadIdx.x < 4 && nsp > 0) {
+    // the split lists run in groups of four: repeat the last split
+    X.aptr[nsp + threadIdx.x] = X.aptr[nsp - 1];
+    X.bptr[nsp + threadIdx.x] = X.bptr[nsp - 1];
+  }
+  if (S == SEMI_VITERBI && J.interleaved == 3 && lane < 16) {
+    // the -inf rows of the flat-tile stage (rows 16 and kStageRowB + 16 of both buffers)
+    const int row = (lane >> 3) * kStageRows + ((lane & 4) ? kStageRowB + 16 : 16);
+    sm.stage[warp * kStageFloats + row * 4 + (lane & 3)] = -CUDART_INF_F;
+  }
   // the cell's gate per segment, one ballot per 32 segments (read after the
   // first barrier below)
   for (int base = 0; base < J.nseg; base += blockDim.x) {
@@ -232,7 +413,10 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       X.la[s][w] = __ldg(X.alive[c0 + s] + w);
       X.lb[s][w] = __ldg(X.blive[c0 + s] + w);
     }
-    if (threadIdx.x == 0) X.nlive = 0;
+    if (threadIdx.x == 0) {
+      X.nlive = 0;
+      X.next = 0;
+    }
     __syncthreads();
     // pl[ca] = union over splits with a live ca on the left of the right-hand live sets
     for (int ca = threadIdx.x; ca < nco; ca += blockDim.x) {
@@ -282,6 +466,11 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
     const int nlive = X.nlive;
+    if (S == SEMI_VITERBI && J.interleaved == 3) {
+      flat_pairs(J, sm, X, c0, nc, nlive, Mw, P, work, corner);
+      __syncthreads();
+      continue;
+    }
     for (int i = X.g * nwarps + warp; i < nlive; i += X.G * nwarps) {
       const int p = sm.list[i];
       const int key = __ldg(J.pair_key + p);
@@ -297,7 +486,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
         // outer product with each split's member values staged in shared
         // memory: per step a lane loads one A and one B member of two live
         // splits, then every task reads its operands from the stage
-        float(*st)[2][32] = reinterpret_cast<float(*)[2][32]>(sm.stage + warp * 128);
+        float(*st)[2][32] = reinterpret_cast<float(*)[2][32]>(sm.stage + warp * kStageFloats);
         // ny, nz <= 16: one load per lane stages both operands (lanes 0-15 the
         // A members, lanes 16-31 the B members) into st[s][0]
         const bool narrow = ny <= 16 && nz <= 16;
@@ -595,11 +784,11 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 
 // ---------------------------------------------------------------------------
 // Inside pass over the cells of a work list (span 1: the unary layer over
-// lexicon cells).  Register budgets: six CTAs per SM (the pair-factored
-// Viterbi instance spills 32 bytes there and is still faster than at five
-// CTAs: the kernel is latency-bound); five for the pair-factored Real pass.
+// lexicon cells).  Register budgets: five CTAs per SM for the pair-factored
+// passes (48 registers: the flat-tile path keeps up to eight tile entries
+// and their stage offsets in registers), six for the target-major ones.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, S == SEMI_REAL && MODE == 2 ? 5 : 6)
+__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
     k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
@@ -918,7 +1107,7 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage) {
   const size_t cs = L.cell_size;
   if (L.mode == 2)
-    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? 128 : 0) + L.max_mtile)) * sizeof(float) +
+    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + L.max_mtile)) * sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int);
   return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);
 }

@@ -38,7 +38,7 @@ struct DevJob {
   int a_is_t, b_is_t;
   int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs):
                           // 1 mixed-target slices, 2 one target per lane slice (slice length a
-                          // multiple of 4)
+                          // multiple of 4), 3 the flat-tile layout below
   const int* pair_key;    // [npair] ca | cb << 8
   const int* pair_gate;   // [npair * mask_size] OR of the pair's segment bits
   const int* pair_blk;    // [npair + 1] block range
@@ -46,6 +46,22 @@ struct DevJob {
   const int* blk_ptr;     // [nblk + 1] rule range, each a multiple of 32 (lane-interleaved, padded)
   const int* blk_nrule;   // [nblk] rules of the block before padding
   const int2* pair_rules;   // {(j * nz + k) | target << 16, bits(w)}
+  // Flat-tile layout (interleaved == 3; Viterbi inside jobs whose every pair
+  // has contiguous operand members, at most 16 per side, and whose blocks
+  // have at most 32 targets).  A pair's outer product M[e], e = j * nz + k,
+  // is held one entry per lane and slot (e = lane + 32 * slot).  A block's
+  // rules keep one target per lane slice; each lane's slice is stored as
+  // records of four rules: their tile entries e (one byte each) and their
+  // weights (padding: weight -inf).  The rules of a record position are
+  // ordered so that the 32 lanes' entries fall in distinct shared-memory
+  // banks where the slices allow.
+  const int4* pair_desc;  // [npair] {first A member | first B member << 16, first block,
+                          //          ny | nz << 8 | blocks << 16, ca | cb << 8}
+  const int4* fr_blk;     // [nblk] {segment, first record, end record, rules}; records of a
+                          // block: 32 lanes x steps
+  const int* fr_tgt;      // [nblk * 32] target of each lane's slice, -1 for none
+  const unsigned* fr_idx; // [records] four tile entries, byte q = rule q
+  const float4* fr_w;     // [records] four weights
 };
 
 struct DevUJob {

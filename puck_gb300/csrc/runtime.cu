@@ -295,6 +295,143 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
   return reinterpret_cast<const T*>(D.upload(h, c * sizeof(T)));
 }
 
+// The flat-tile layout of a Viterbi inside job (DevJob::pair_desc, fr_*):
+// built when every pair's operand members are contiguous index ranges of at
+// most 16 symbols per side and every block has at most 32 targets.  Each
+// target of a block gets lanes in proportion to its rule count (at least
+// one); a lane's slice is stored as records of four rules, padded with
+// weight -inf (the max-plus zero, which never changes a cell).
+// Returns false, uploading nothing, when the job does not qualify.
+bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int64_t npk, const int* pk,
+                      const int* pbk, const int* bs, const int* bp, const int* pr, const float* pw) {
+  static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
+  static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
+  const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+  const int* am = L.get<int>(a_t[j] ? "t_mem" : "nt_mem", "i4", nullptr);
+  const int* bo = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
+  const int* bm = L.get<int>(b_t[j] ? "t_mem" : "nt_mem", "i4", nullptr);
+  auto contiguous = [](const int* off, const int* mem, int c) {
+    for (int i = off[c]; i < off[c + 1]; ++i)
+      if (mem[i] != mem[off[c]] + (i - off[c])) return false;
+    return true;
+  };
+  std::vector<int4> desc(std::max<int64_t>(npk, 1));
+  for (int64_t k = 0; k < npk; ++k) {
+    const int ca = pk[k] & 255, cb = (pk[k] >> 8) & 255;
+    const int ny = ao[ca + 1] - ao[ca], nz = bo[cb + 1] - bo[cb];
+    if (ny < 1 || nz < 1 || ny > 16 || nz > 16 || !contiguous(ao, am, ca) || !contiguous(bo, bm, cb)) return false;
+    if (pbk[k + 1] - pbk[k] > 65535) return false;
+    desc[k] = make_int4(am[ao[ca]] | bm[bo[cb]] << 16, pbk[k], ny | nz << 8 | (pbk[k + 1] - pbk[k]) << 16,
+                        ca | cb << 8);
+  }
+  const int nblk = npk > 0 ? pbk[npk] : 0;
+  std::vector<int> tgt((size_t)std::max(nblk, 1) * 32, -1);
+  std::vector<int4> blk((size_t)std::max(nblk, 1), make_int4(0, 0, 0, 0));
+  std::vector<unsigned> idx;
+  std::vector<float4> w;
+  for (int64_t k = 0; k < npk; ++k) {
+    const int nz = (desc[k].z >> 8) & 255;
+    for (int b = pbk[k]; b < pbk[k + 1]; ++b) {
+      const int r0 = bp[b], cnt = bp[b + 1] - bp[b];
+      // targets of the block (its rules are sorted by target) and their lanes
+      std::vector<int> tstart, tcnt, tlanes;
+      for (int r = 0; r < cnt; ++r)
+        if (r == 0 || ((unsigned)pr[r0 + r] >> 16) != ((unsigned)pr[r0 + r - 1] >> 16)) tstart.push_back(r);
+      if (tstart.size() > 32) return false;
+      for (size_t t = 0; t < tstart.size(); ++t) tcnt.push_back((t + 1 < tstart.size() ? tstart[t + 1] : cnt) - tstart[t]);
+      tlanes.assign(tstart.size(), 1);
+      auto slice = [&](size_t t) { return (tcnt[t] + tlanes[t] - 1) / tlanes[t]; };
+      for (int free_lanes = 32 - (int)tstart.size(); free_lanes > 0 && !tstart.empty(); --free_lanes) {
+        size_t best = 0;
+        for (size_t t = 1; t < tstart.size(); ++t)
+          if (slice(t) > slice(best)) best = t;
+        if (slice(best) <= 1) break;
+        ++tlanes[best];
+      }
+      int per = 0;
+      for (size_t t = 0; t < tstart.size(); ++t) per = std::max(per, slice(t));
+      const int steps = (per + 3) / 4, slots = 4 * steps;
+      // each lane's rules (tile entry, weight), in any order: max is commutative
+      std::vector<std::vector<std::pair<int, float>>> todo(32);
+      int lane = 0;
+      for (size_t t = 0; t < tstart.size(); ++t) {
+        const int len = slice(t);
+        for (int l = 0; l < tlanes[t]; ++l, ++lane) {
+          const int a0 = tstart[t] + l * len, a1 = std::min(tstart[t] + tcnt[t], a0 + len);
+          tgt[(size_t)b * 32 + lane] = (int)((unsigned)pr[r0 + tstart[t]] >> 16);
+          for (int r = a0; r < a1; ++r) {
+            const int x = pr[r0 + r];
+            todo[lane].push_back({(x & 255) * nz + ((x >> 8) & 255), pw[r0 + r]});
+          }
+        }
+      }
+      // Each slot (one of the four loads of a record) is one warp-wide shared
+      // load of M: its 32 tile entries should fall in distinct banks (e mod
+      // 32), or read the same entry.  Slot by slot, lanes that must take a
+      // rule now (as many rules left as slots) pick first; the others take a
+      // rule only in a bank still free.  A lane without a rule this slot
+      // reads an entry already read by the slot (weight -inf).
+      const size_t base = idx.size();
+      idx.resize(base + (size_t)steps * 32, 0u);
+      w.resize(base + (size_t)steps * 32, make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
+      for (int sl = 0; sl < slots; ++sl) {
+        int bank_e[32];
+        std::fill(bank_e, bank_e + 32, -1);
+        int pick[32];
+        std::fill(pick, pick + 32, -1);
+        auto choose = [&](int l, bool forced) {
+          auto& v = todo[l];
+          int best = -1;
+          for (size_t r = 0; r < v.size(); ++r) {
+            const int e = v[r].first, bk = e & 31;
+            if (bank_e[bk] < 0 || bank_e[bk] == e) {
+              best = (int)r;
+              break;
+            }
+          }
+          if (best < 0 && forced) best = 0;
+          if (best < 0) return;
+          pick[l] = best;
+          const int e = v[best].first;
+          if (bank_e[e & 31] < 0) bank_e[e & 31] = e;
+        };
+        for (int l = 0; l < 32; ++l)
+          if (!todo[l].empty() && (int)todo[l].size() >= slots - sl) choose(l, true);
+        for (int l = 0; l < 32; ++l)
+          if (pick[l] < 0 && !todo[l].empty() && (int)todo[l].size() < slots - sl) choose(l, false);
+        int any_e = 0;
+        for (int k = 0; k < 32; ++k)
+          if (bank_e[k] >= 0) {
+            any_e = bank_e[k];
+            break;
+          }
+        for (int l = 0; l < 32; ++l) {
+          const size_t at = base + (size_t)(sl / 4) * 32 + l;
+          int e = any_e;
+          float wt = -INFINITY;
+          if (pick[l] >= 0) {
+            e = todo[l][pick[l]].first;
+            wt = todo[l][pick[l]].second;
+            todo[l].erase(todo[l].begin() + pick[l]);
+          }
+          idx[at] |= (unsigned)e << (8 * (sl % 4));
+          (&w[at].x)[sl % 4] = wt;
+        }
+      }
+      for (int l = 0; l < 32; ++l)
+        if (!todo[l].empty()) return false;  // cannot happen: every lane has slots for all its rules
+      if (idx.size() > (size_t)INT32_MAX) return false;
+      blk[b] = make_int4(bs[b], (int)base, (int)idx.size(), cnt);
+    }
+  }
+  J.pair_desc = static_cast<const int4*>(D.upload(desc.data(), desc.size() * sizeof(int4)));
+  J.fr_blk = static_cast<const int4*>(D.upload(blk.data(), blk.size() * sizeof(int4)));
+  J.fr_tgt = static_cast<const int*>(D.upload(tgt.data(), tgt.size() * sizeof(int)));
+  J.fr_idx = static_cast<const unsigned*>(D.upload(idx.data(), idx.size() * sizeof(unsigned)));
+  J.fr_w = static_cast<const float4*>(D.upload(w.data(), w.size() * sizeof(float4)));
+  return true;
+}
+
 }  // namespace
 
 void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
@@ -459,6 +596,9 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     if (rr.size() > (size_t)INT32_MAX) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule table too large in " + n};
     J.npair = (int)npk;
     J.interleaved = !interleave ? 0 : one_target_lanes ? 2 : 1;
+    if (J.interleaved == 2 &&
+        build_flat_tiles(D, J, L, j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw))
+      J.interleaved = 3;
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
