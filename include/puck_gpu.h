@@ -103,6 +103,27 @@ puck_status puck_grammar_level_info(const puck_grammar* g, int32_t level, int32_
 /* Word string -> id in the vocabulary of the fine level; -1 if unknown. */
 int32_t puck_grammar_word_id(const puck_grammar* g, const char* word);
 
+/* --- grammar compiler (CompileGrammar.main, CompileGrammar.scala:20-72) -- */
+/* Options of CompileGrammar (CompileGrammar.scala:20-25). */
+typedef struct puck_compile_options {
+  int32_t viterbi;    /* --viterbi (default 1): the fine level's semiring is Viterbi */
+  int32_t logsum;     /* --logsum: with viterbi = 0, LogSum instead of Real (CompileGrammar.scala:45-51) */
+  int32_t reproject;  /* --reproject: not supported (PUCK_ERR_INVALID_ARG) */
+  float threshold;    /* rules and lexicon entries with a lower log score are dropped (-12, as
+                         CompileGrammar.scala:56 passes to parseBerkeleyText) */
+} puck_compile_options;
+void puck_default_compile_options(puck_compile_options* opts);
+/* Compiles the Berkeley text grammars named by text_prefixes ("a:b", coarse
+ * level first; each prefix has .numstates, .binary, .unary, .lexicon) into
+ * the grammar.grz at out_grz, as `CompileGrammar --textGrammarPrefix a:b
+ * --grammar out.grz` does (CLParserData.make + writeSequence,
+ * CLParser.scala:1264-1285,1307-1317).  Coarse levels are Viterbi.  The
+ * compiler is the library's host-side Python package, run in an embedded
+ * CPython interpreter (the caller's, or libpython3.12 loaded on first use).
+ * opts may be NULL (defaults).  Returns PUCK_ERR_BAD_GRAMMAR with a message
+ * when the text grammars cannot be read. */
+puck_status puck_compile_grammar(const char* text_prefixes, const char* out_grz, const puck_compile_options* opts);
+
 /* --- parser (new CLParser / release, CLParser.scala:46-89) -------------- */
 puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts, puck_status* status);
 void puck_parser_destroy(puck_parser* p);

@@ -50,7 +50,7 @@ class ServerStats(ctypes.Structure):
                 ("h2d_bytes", ctypes.c_int64), ("d2h_bytes", ctypes.c_int64)]
 
 
-EXPORTS = ("puck_default_options", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
+EXPORTS = ("puck_default_options", "puck_default_compile_options", "puck_compile_grammar", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
            "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
            "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_parser_tensor_cores", "puck_mbr_decode_static",

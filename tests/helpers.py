@@ -71,3 +71,32 @@ def node_blocks(nodes, lengths):
         out.append(nodes[start:start + k])
         start += k
     return out
+
+
+def write_text_grammar(directory, name, splits, seed=0):
+    """A small Berkeley-format text grammar (``<name>.numstates``, ``.binary``,
+    ``.unary``, ``.lexicon``) with ``splits`` substates per label: ROOT -> S,
+    S -> NP VP, NP -> DT NN, VP -> VB NP, six words.  Returns the prefix."""
+    rng = np.random.default_rng(seed)
+    labels = {"ROOT": 1, "S": splits, "NP": splits, "VP": splits, "DT": splits, "NN": splits, "VB": splits}
+    prefix = os.path.join(directory, name)
+    with open(prefix + ".numstates", "w") as f:
+        for lab, k in labels.items():
+            f.write(f"{lab}\t{k}\n")
+    with open(prefix + ".binary", "w") as f:
+        for p, l, r in (("S", "NP", "VP"), ("NP", "DT", "NN"), ("VP", "VB", "NP")):
+            for i in range(labels[p]):
+                w = rng.dirichlet(np.ones(labels[l] * labels[r]))
+                for j in range(labels[l]):
+                    for k in range(labels[r]):
+                        f.write(f"{p}_{i} {l}_{j} {r}_{k} {w[j * labels[r] + k]:.6g}\n")
+    with open(prefix + ".unary", "w") as f:
+        w = rng.dirichlet(np.ones(labels["S"]))
+        for j in range(labels["S"]):
+            f.write(f"ROOT_0 S_{j} {w[j]:.6g}\n")
+    with open(prefix + ".lexicon", "w") as f:
+        for tag, words in (("DT", ("the", "a")), ("NN", ("dog", "cat")), ("VB", ("sees", "chases"))):
+            for wd in words:
+                probs = ", ".join(f"{x:.6g}" for x in rng.uniform(0.05, 0.5, size=labels[tag]))
+                f.write(f"{tag} {wd} [{probs}]\n")
+    return prefix

@@ -317,3 +317,28 @@ def test_gpu_matches_golden_fixture(case):
             assert np.array_equal(bits(z), bits(data["partitions"]))
     if "masks" in data:
         assert np.array_equal(P.debug_copy(0, "masks"), data["masks"])
+
+
+def test_compile_then_parse_through_the_c_abi(tmp_path):
+    """CompileGrammar and CLParser both through the C ABI: text grammars ->
+    puck_compile_grammar -> puck_grammar_load / puck_parse, trees
+    bit-identical to the oracle's parse of the same archive."""
+    import ctypes
+    from helpers import write_text_grammar
+    from puck_gb300 import _lib, grz
+    c = write_text_grammar(str(tmp_path), "coarse", 1, seed=5)
+    f = write_text_grammar(str(tmp_path), "fine", 4, seed=6)
+    out = str(tmp_path / "abi.grz")
+    L = _lib.load()
+    L.puck_compile_grammar.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p]
+    assert L.puck_compile_grammar(f"{c}:{f}".encode(), out.encode(), None) == 0, _lib.last_error()
+    P = CLParser(out, max_alloc_size=1 << 30)
+    text = ["the dog sees a cat", "a cat chases the dog", "the cat sees the dog"]
+    sents = [np.array(P.word_ids(t.split()), np.int32) for t in text]
+    assert all((s >= 0).all() for s in sents)
+    words, offsets, _ = pack_sentences(sents)
+    nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all()
+    r = oracle.run(grz.read_sequence(out, load_arrays=True), sents, mode="parse")
+    assert np.array_equal(nodes, r.trees())
+    assert P.parse([t.split() for t in text])[0].is_success

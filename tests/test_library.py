@@ -87,3 +87,81 @@ def test_bad_artifacts_fail_cleanly(tmp_path):
 
 def test_build_flags_target_sm103a():
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _compile_via_abi(prefixes, out, viterbi=1, logsum=0):
+    L = _lib.load()
+    L.puck_compile_grammar.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_void_p]
+    L.puck_compile_grammar.restype = ctypes.c_int32
+    opts = (ctypes.c_int32 * 4)()
+    L.puck_default_compile_options(ctypes.byref(opts))
+    opts[0], opts[1] = viterbi, logsum
+    return L.puck_compile_grammar(prefixes.encode(), out.encode(), ctypes.byref(opts))
+
+
+def _same_archives(a, b):
+    import zipfile
+    za, zb = zipfile.ZipFile(a), zipfile.ZipFile(b)
+    names = sorted(za.namelist())
+    assert names == sorted(zb.namelist())
+    for n in names:
+        assert za.read(n) == zb.read(n), n
+
+
+def test_compile_grammar_through_the_c_abi_matches_the_python_compiler(tmp_path):
+    """puck_compile_grammar (CompileGrammar behind the C ABI) writes the same
+    archive, entry for entry, as the compile_grammar program, for a Viterbi
+    and a LogSum fine level, and reports unreadable input as BAD_GRAMMAR."""
+    from helpers import write_text_grammar
+    from puck_gb300 import compile_grammar
+    c = write_text_grammar(str(tmp_path), "coarse", 1, seed=1)
+    f = write_text_grammar(str(tmp_path), "fine", 2, seed=2)
+    for vit, ls, sem in ((1, 0, "viterbi"), (0, 1, "logsum")):
+        abi, py = str(tmp_path / f"abi_{sem}.grz"), str(tmp_path / f"py_{sem}.grz")
+        assert _compile_via_abi(f"{c}:{f}", abi, vit, ls) == 0, _lib.last_error()
+        assert compile_grammar.main(["--textGrammarPrefix", f"{c}:{f}", "--grammar", py,
+                                     "--viterbi", str(bool(vit)).lower(), "--logsum", str(bool(ls)).lower()]) == 0
+        _same_archives(abi, py)
+    assert _compile_via_abi(str(tmp_path / "missing"), str(tmp_path / "x.grz")) == 2
+    assert "missing" in _lib.last_error()
+    L = _lib.load()
+    opts = (ctypes.c_int32 * 4)()
+    L.puck_default_compile_options(ctypes.byref(opts))
+    opts[2] = 1  # reproject
+    assert L.puck_compile_grammar(f"{c}:{f}".encode(), str(tmp_path / "r.grz").encode(), ctypes.byref(opts)) == 6
+
+
+def test_compile_grammar_from_a_host_without_python(tmp_path):
+    """A C host that loads only libpuck_gb300.so (no Python in the process,
+    like a JVM): puck_compile_grammar starts its own interpreter and writes
+    the same archive."""
+    import shutil
+    import subprocess
+    from helpers import write_text_grammar
+    from puck_gb300 import compile_grammar
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    c = write_text_grammar(str(tmp_path), "coarse", 1, seed=3)
+    f = write_text_grammar(str(tmp_path), "fine", 3, seed=4)
+    src = tmp_path / "host.c"
+    src.write_text(
+        '#include <dlfcn.h>\n#include <stdio.h>\n#include "puck_gpu.h"\n'
+        "int main(int argc, char** argv) {\n"
+        "  void* h = dlopen(argv[1], RTLD_NOW);\n"
+        "  if (!h) { fprintf(stderr, \"%s\\n\", dlerror()); return 3; }\n"
+        "  puck_status (*compile)(const char*, const char*, const puck_compile_options*) =\n"
+        "      (puck_status (*)(const char*, const char*, const puck_compile_options*))dlsym(h, \"puck_compile_grammar\");\n"
+        "  size_t (*err)(char*, size_t) = (size_t (*)(char*, size_t))dlsym(h, \"puck_last_error\");\n"
+        "  puck_status st = compile(argv[2], argv[3], NULL);\n"
+        "  char msg[512]; msg[0] = 0; if (st) err(msg, sizeof msg);\n"
+        "  printf(\"%d %s\\n\", (int)st, msg);\n"
+        "  return st == PUCK_OK ? 0 : 1;\n}\n")
+    exe = tmp_path / "host"
+    subprocess.check_call(["gcc", "-O1", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-ldl"])
+    out = str(tmp_path / "c_host.grz")
+    r = subprocess.run([str(exe), build.build(), f"{c}:{f}", out], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    py = str(tmp_path / "py.grz")
+    assert compile_grammar.main(["--textGrammarPrefix", f"{c}:{f}", "--grammar", py]) == 0
+    _same_archives(out, py)
