@@ -21,12 +21,12 @@
 //   semirings           src/main/scala/puck/parser/RuleSemiring.scala:22-98
 //   lexicon scoring     CLParser.scala:411-467
 //   masks               src/main/scala/puck/parser/gen/CLMaskKernels.scala:172-236
-//   scaling             src/main/scala/puck/parser/gen/CLScalingKernels.scala:225-243
-//   root scores         src/main/scala/puck/parser/gen/CLParserUtils.scala:305-316
+//   scaling             src/main/scala/puck/parser/gen/CLScalingKernels.scala:51-69
+//   root scores         src/main/scala/puck/parser/gen/CLParserUtils.scala:64-78
 //   Viterbi backtrace   src/main/scala/puck/parser/gen/CLViterbi.scala:383-605 (WG_SIZE = 1)
 //   MBR                 src/main/scala/puck/parser/gen/CLMBRKernels.scala:118-170 + CLParser.scala:587-696
 //   partitions          CLParser.scala:189-206
-//   chart indexing      src/main/scala/puck/parser/ParseChart.scala:58-65, Batch.scala:218-253
+//   chart indexing      src/main/scala/puck/parser/ParseChart.scala:58-65, Batch.scala:23,50-58
 //
 // The engine is templated on the float type: F = float is the bit-level
 // restatement; F = double is the FP64 reference of the same computation.
@@ -550,8 +550,11 @@ void mbr_extract(const Batch& B, int s, const std::vector<float>& score, const s
       float topScaled = score[B.top(s, begin, end)];
       float botScaled = score[B.bot(s, begin, end)];
       if (scaling) {
-        topScaled *= (float)std::exp((double)itop(begin, end) + otop(begin, end) - itop(0, n));
-        botScaled *= (float)std::exp((double)ibot(begin, end) + obot(begin, end) - itop(0, n));
+        // FP32 sum of the scales, math.exp in FP64, rounded to FP32 (CLParser.scala:613-614)
+        const float at = (itop(begin, end) + otop(begin, end)) - itop(0, n);
+        const float ab = (ibot(begin, end) + obot(begin, end)) - itop(0, n);
+        topScaled *= (float)std::exp((double)at);
+        botScaled *= (float)std::exp((double)ab);
       }
       if (std::isnan(topScaled)) topScaled = 0.f;
       if (std::isnan(botScaled)) botScaled = 0.f;

@@ -1,5 +1,5 @@
 """``python -m puck_gb300.compile_grammar`` -- the reference's CompileGrammar
-(src/main/scala/puck/parser/CompileGrammar.scala:20-79) for this library.
+(src/main/scala/puck/parser/CompileGrammar.scala:20-72) for this library.
 
 Same flags and meaning: ``--textGrammarPrefix a:b`` (Berkeley text grammars,
 coarse first), ``--grammar out.grz``, ``--viterbi`` (default true; the fine

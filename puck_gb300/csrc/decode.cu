@@ -3,11 +3,11 @@
 //
 // Reference semantics restated (dlwh/puck paths):
 //   masks         src/main/scala/puck/parser/gen/CLMaskKernels.scala:172-236
-//   scaling       src/main/scala/puck/parser/gen/CLScalingKernels.scala:225-243
+//   scaling       src/main/scala/puck/parser/gen/CLScalingKernels.scala:51-69
 //   backtrace     src/main/scala/puck/parser/gen/CLViterbi.scala:383-605
 //   MBR           src/main/scala/puck/parser/gen/CLMBRKernels.scala:118-170,
 //                 src/main/scala/puck/parser/CLParser.scala:587-696
-//   root scores   src/main/scala/puck/parser/gen/CLParserUtils.scala:305-316,
+//   root scores   src/main/scala/puck/parser/gen/CLParserUtils.scala:64-78,
 //                 CLParser.scala:189-206
 
 #include "mbr_dp.cuh"

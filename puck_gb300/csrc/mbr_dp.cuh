@@ -26,8 +26,12 @@ __device__ inline void mbr_decode_sentence(int n, long long off, const float2* d
       const long long ct = toff + chart_index(bg, en, n), cb = off + chart_index(bg, en, n);
       float topS = decode[ct].x, botS = decode[cb].x;
       if (scaling) {
-        topS *= (float)exp((double)iscale[ct] + (double)oscale[ct] - (double)root_i);
-        botS *= (float)exp((double)iscale[cb] + (double)oscale[cb] - (double)root_i);
+        // CLParser.scala:613-614: the scales are summed in FP32 (Scala Float
+        // arithmetic), exponentiated with math.exp in FP64 and rounded to
+        // FP32; the one FP64 exp per cell reproduces that factor
+        const float at = (iscale[ct] + oscale[ct]) - root_i, ab = (iscale[cb] + oscale[cb]) - root_i;
+        topS *= (float)exp((double)at);
+        botS *= (float)exp((double)ab);
       }
       if (isnan(topS)) topS = 0.f;
       if (isnan(botS)) botS = 0.f;

@@ -388,12 +388,12 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
   float* Mw = sm.M + warp * L.max_mtile;
   const int nsp = X.nsp;
   unsigned long long work = 0, corner = 0;
-  if (S == SEMI_VITERBI && J.interleaved == 3 && threadIdx.x < 4 && nsp > 0) {
+  if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage && threadIdx.x < 4 && nsp > 0) {
     // the split lists run in groups of four: repeat the last split
     X.aptr[nsp + threadIdx.x] = X.aptr[nsp - 1];
     X.bptr[nsp + threadIdx.x] = X.bptr[nsp - 1];
   }
-  if (S == SEMI_VITERBI && J.interleaved == 3 && lane < 16) {
+  if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage && lane < 16) {
     // the -inf rows of the flat-tile stage (rows 16 and kStageRowB + 16 of both buffers)
     const int row = (lane >> 3) * kStageRows + ((lane & 4) ? kStageRowB + 16 : 16);
     sm.stage[warp * kStageFloats + row * 4 + (lane & 3)] = -CUDART_INF_F;
@@ -466,7 +466,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
     const int nlive = X.nlive;
-    if (S == SEMI_VITERBI && J.interleaved == 3) {
+    if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage) {
       flat_pairs(J, sm, X, c0, nc, nlive, Mw, P, work, corner);
       __syncthreads();
       continue;
@@ -482,7 +482,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       const int a0 = __ldg(aoff + ca), ny = __ldg(aoff + ca + 1) - a0;
       const int b0 = __ldg(boff + cb), nz = __ldg(boff + cb + 1) - b0;
       const int nkq = (nz + 3) >> 2, ntask = ny * nkq;
-      if (S == SEMI_VITERBI && J.interleaved && ntask <= 64 && ny <= 32 && nz <= 32) {
+      if (S == SEMI_VITERBI && J.interleaved && sm.stage && ntask <= 64 && ny <= 32 && nz <= 32) {
         // outer product with each split's member values staged in shared
         // memory: per step a lane loads one A and one B member of two live
         // splits, then every task reads its operands from the stage

@@ -123,7 +123,7 @@ struct DevTc {
 
 // Sentences of a batch (or of a server's resident set).  Each sentence's
 // chart is laid out like the reference's Batch (src/main/scala/puck/parser/
-// Batch.scala:218-253): a bot half then a top half of n(n+1)/2 cells each, in
+// Batch.scala:23,50-58): a bot half then a top half of n(n+1)/2 cells each, in
 // span-major chartIndex order, starting at cell_off[s].  In batch mode the
 // sentences are packed back to back; a server places them anywhere in its
 // resident chart arena.

@@ -302,8 +302,8 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
 // one); a lane's slice is stored as records of four rules, padded with
 // weight -inf (the max-plus zero, which never changes a cell).
 // Returns false, uploading nothing, when the job does not qualify.
-bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int64_t npk, const int* pk,
-                      const int* pbk, const int* bs, const int* bp, const int* pr, const float* pw) {
+bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int ntgt, int64_t npk,
+                      const int* pk, const int* pbk, const int* bs, const int* bp, const int* pr, const float* pw) {
   static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
   static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
   const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
@@ -330,7 +330,7 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, i
   std::vector<unsigned> idx;
   std::vector<float4> w;
   for (int64_t k = 0; k < npk; ++k) {
-    const int nz = (desc[k].z >> 8) & 255;
+    const int ny = desc[k].z & 255, nz = (desc[k].z >> 8) & 255;
     for (int b = pbk[k]; b < pbk[k + 1]; ++b) {
       const int r0 = bp[b], cnt = bp[b + 1] - bp[b];
       // targets of the block (its rules are sorted by target) and their lanes
@@ -420,6 +420,13 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, i
       }
       for (int l = 0; l < 32; ++l)
         if (!todo[l].empty()) return false;  // cannot happen: every lane has slots for all its rules
+      // every tile entry inside the pair's tile (a byte each), every target
+      // below the job's target count
+      for (size_t q = base; q < idx.size(); ++q)
+        for (int c = 0; c < 4; ++c)
+          if ((int)((idx[q] >> (8 * c)) & 255u) >= ny * nz) return false;
+      for (int l = 0; l < 32; ++l)
+        if (tgt[(size_t)b * 32 + l] >= ntgt) return false;
       if (idx.size() > (size_t)INT32_MAX) return false;
       blk[b] = make_int4(bs[b], (int)base, (int)idx.size(), cnt);
     }
@@ -484,12 +491,19 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     // its operand pair in the pair's row-major outer-product tile.
     const float zero = L.semiring == puck::SEMI_REAL ? 0.f : -INFINITY;
     const int* pbk = L.get<int>(n + "/pair_blk", "i4", nullptr);
+    // nz (and ny) of every block, from the member lists of the operand roles
+    // the device uses for this job (DevJob::a_is_t / b_is_t = a_t[j] / b_t[j])
+    const int* ao_ = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
     const int* bo_ = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
-    std::vector<int> blk_nz(nbp > 0 ? nbp - 1 : 0, 1);
+    std::vector<int> blk_nz(nbp > 0 ? nbp - 1 : 0, 1), blk_ny(nbp > 0 ? nbp - 1 : 0, 1);
     for (int64_t k = 0; k < npk; ++k) {
-      const int cb = (pk[k] >> 8) & 255;
-      for (int b = pbk[k]; b < pbk[k + 1]; ++b) blk_nz[b] = bo_[cb + 1] - bo_[cb];
+      const int ca = pk[k] & 255, cb = (pk[k] >> 8) & 255;
+      for (int b = pbk[k]; b < pbk[k + 1]; ++b) {
+        blk_nz[b] = bo_[cb + 1] - bo_[cb];
+        blk_ny[b] = ao_[ca + 1] - ao_[ca];
+      }
     }
+    const int ntgt_j = (int)(nrow - 1);
     std::vector<int2> rr;
     std::vector<int> dev_bp(1, 0), blk_n;
     // Outside jobs and sum-product levels keep the archive's layout: blocks
@@ -590,6 +604,14 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
           rr[base + slot] = v;
         }
       }
+      // every word the device decodes from this block: the tile index below
+      // the pair's ny * nz (the warp's M tile holds max_mtile >= that) and
+      // the target below the job's target count (<= cell_size)
+      for (size_t q = base; q < rr.size(); ++q) {
+        const unsigned x = (unsigned)rr[q].x;
+        if ((int)(x & 0xffffu) >= blk_ny[b] * nz || (int)(x >> 16) >= ntgt_j)
+          throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule out of its tile or target range in " + n};
+      }
       dev_bp.push_back((int)rr.size());
       blk_n.push_back(cnt);
     }
@@ -597,7 +619,7 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.npair = (int)npk;
     J.interleaved = !interleave ? 0 : one_target_lanes ? 2 : 1;
     if (J.interleaved == 2 &&
-        build_flat_tiles(D, J, L, j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw))
+        build_flat_tiles(D, J, L, j, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw))
       J.interleaved = 3;
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];

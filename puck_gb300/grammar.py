@@ -17,7 +17,7 @@ compile-time logic (paths are relative to the dlwh/puck project):
   with ``MIN_SINGLE_COARSE_PARENT_GROUP_SIZE = 300`` and ``NUM_SM = 8``
   sub-segments.  A segment's coarse-parent bitset gates it per chart cell
   (src/main/scala/puck/parser/CLParser.scala:845-855).
-* outside rule rotations -- src/main/scala/puck/parser/gen/CLOutside.scala:168-207.
+* outside rule rotations -- src/main/scala/puck/parser/gen/CLOutside.scala:61-71 (rotations), 73-112 (the rotated jobs).
 * Viterbi backtrace tables -- src/main/scala/puck/parser/gen/CLViterbi.scala:274-353,610-628.
 
 Symbol order: the reference orders symbols by the bundled ``symbols_dump``
@@ -47,7 +47,7 @@ NUM_SUBSEGMENTS = 8
 
 # Inside jobs: (bucket) -> target is the parent.  Outside jobs rotate a
 # bucket's rules so that the updated child becomes the "parent"
-# (CLOutside.scala:168-178).  Each job records the index space of its target
+# (CLOutside.scala:61-67).  Each job records the index space of its target
 # and of the two operands that are added before the rule score:
 # value = (A[ia] + B[ib]) + w.
 #                 name     bucket rotate  tgt_is_t a_is_t b_is_t
