@@ -628,7 +628,8 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.pair_blk = up<int>(D, L, n + "/pair_blk", "i4");
     J.blk_seg = up<int>(D, L, n + "/blk_seg", "i4");
     J.blk_ptr = static_cast<const int*>(D.upload(dev_bp.data(), dev_bp.size() * sizeof(int)));
-    J.blk_nrule = static_cast<const int*>(D.upload(blk_n.data(), std::max<size_t>(blk_n.size(), 1) * sizeof(int)));
+    if (blk_n.empty()) blk_n.push_back(0);  // a job without rules still gets a (never read) table
+    J.blk_nrule = static_cast<const int*>(D.upload(blk_n.data(), blk_n.size() * sizeof(int)));
     J.pair_rules = reinterpret_cast<const int2*>(D.upload(rr.data(), rr.size() * sizeof(int2)));
     d.max_npair = std::max(d.max_npair, J.npair);
     const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
