@@ -42,6 +42,9 @@ constexpr int kRuleBatch = 4;   // rules per lane whose loads are in flight toge
 constexpr int kStageRows = 34;
 constexpr int kStageFloats = 2 * kStageRows * 4;
 constexpr int kStageRowB = 17;
+// Per-warp list of a pair's live splits (chunk positions, one byte each),
+// padded by three repeats of the last one for the groups of four.
+constexpr int kSplitList = 68;
 
 // Shared bookkeeping of one target cell.
 struct __align__(16) CellCtx {
@@ -77,6 +80,7 @@ struct Smem {
   float* stage;  // per warp kStageFloats: staged A and B members of four splits (16-byte aligned)
   unsigned* pl;
   int* list;
+  unsigned char* slist;  // per warp kSplitList: the live splits of the warp's current pair (flat-tile path)
 };
 
 // with_stage: the per-warp operand stage of the Viterbi inside pass
@@ -89,6 +93,7 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
   m.stA = m.stB = m.M = m.stage = nullptr;
   m.pl = nullptr;
   m.list = nullptr;
+  m.slist = nullptr;
   if (L.mode == 2) {
     if (with_stage) {
       m.stage = rest;
@@ -97,6 +102,7 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
     m.M = rest;
     m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * L.max_mtile);
     m.list = reinterpret_cast<int*>(m.pl + L.n_coarse * L.mask_size);
+    if (with_stage) m.slist = reinterpret_cast<unsigned char*>(m.list + L.max_npair);
   } else {
     m.stA = rest;
     m.stB = rest + chunk * cs;
@@ -230,26 +236,25 @@ __device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned lon
 }
 
 // This lane's operand value for each of the four splits of group g (see
-// flat_outer): two 16-byte loads fetch the four row pointers.
-__device__ __forceinline__ float4 load_group(const float* const* rows, int g, unsigned src, bool ok) {
-  const float* p[4];
-  *reinterpret_cast<longlong2*>(&p[0]) = *reinterpret_cast<const longlong2*>(rows + 4 * g);
-  *reinterpret_cast<longlong2*>(&p[2]) = *reinterpret_cast<const longlong2*>(rows + 4 * g + 2);
+// flat_outer): one 4-byte load fetches the group's split positions from the
+// warp's live-split list, then their row pointers.
+__device__ __forceinline__ float4 load_group(const float* const* rows, const unsigned char* sl, int g, unsigned src,
+                                             bool ok) {
+  const unsigned q = *reinterpret_cast<const unsigned*>(sl + 4 * g);
   float4 v;
-  v.x = ok ? __ldg(p[0] + src) : -CUDART_INF_F;
-  v.y = ok ? __ldg(p[1] + src) : -CUDART_INF_F;
-  v.z = ok ? __ldg(p[2] + src) : -CUDART_INF_F;
-  v.w = ok ? __ldg(p[3] + src) : -CUDART_INF_F;
+  v.x = ok ? __ldg(rows[q & 255u] + src) : -CUDART_INF_F;
+  v.y = ok ? __ldg(rows[(q >> 8) & 255u] + src) : -CUDART_INF_F;
+  v.z = ok ? __ldg(rows[(q >> 16) & 255u] + src) : -CUDART_INF_F;
+  v.w = ok ? __ldg(rows[q >> 24] + src) : -CUDART_INF_F;
   return v;
 }
 
 // Outer product of one pair in the flat-tile layout (DevJob::pair_desc): lane
 // slot i holds tile entry e = lane + 32 * i = j * nz + k, i < NS, and ends
-// with max over the chunk's splits s of fl(A_s[Y_j] + B_s[Z_k]), which it
-// stores to the warp's M tile.  Splits go in groups of four consecutive
-// allowed splits; a group with no split live for the pair (mask m) is
-// skipped, and a dead split inside a live group adds only -inf terms.  Per
-// group, lanes 0-15 stage the A members of the four splits as one float4 row
+// with max over the pair's live splits s of fl(A_s[Y_j] + B_s[Z_k]), which
+// it stores to the warp's M tile.  The n live splits (the warp's list sl,
+// padded by repeats of the last one: max is idempotent) go in groups of
+// four.  Per group, lanes 0-15 stage the A members of the four splits as one float4 row
 // each, lanes 16-31 the B members; each slot then reads its two rows (one
 // 16-byte load each) and folds four sums into its entry with two packed adds
 // and two 3-input maxes.  The operand loads of the next live group are
@@ -257,8 +262,8 @@ __device__ __forceinline__ float4 load_group(const float* const* rows, int g, un
 // two stage buffers.  Slots past the tile read the -inf rows and are not
 // stored.
 template <int NS>
-__device__ __forceinline__ void flat_outer(const CellCtx& X, int c0, unsigned long long m, int4 D, float4* st4,
-                                           float* Mw) {
+__device__ __forceinline__ void flat_outer(const CellCtx& X, int c0, const unsigned char* sl, int n, int4 D,
+                                           float4* st4, float* Mw) {
   const int lane = threadIdx.x & 31;
   const int ny = D.z & 255, nz = (D.z >> 8) & 255, E = ny * nz;
   // j = lane / nz, k = lane % nz; then 32 entries further per slot.  The
@@ -287,16 +292,16 @@ __device__ __forceinline__ void flat_outer(const CellCtx& X, int c0, unsigned lo
   const unsigned src = (a_side ? (unsigned)D.x & 0xffffu : (unsigned)D.x >> 16) + mem;
   const float* const* rows = (a_side ? X.aptr : X.bptr) + c0;
   const int my_row = a_side ? mem : kStageRowB + mem;
-  int g = (__ffsll(m) - 1) >> 2;  // first live group (m != 0)
-  float4 v = load_group(rows, g, src, ok);
+  int g = 0;
+  float4 v = load_group(rows, sl, 0, src, ok);
   for (int buf = 0;; buf ^= 1) {
     float4* sb = st4 + buf * kStageRows;
     sb[my_row] = v;
     __syncwarp();
-    const unsigned long long rest = g < 15 ? m >> (4 * g + 4) : 0ull;
+    const bool rest = 4 * (g + 1) < n;
     if (rest) {
-      g += 1 + ((__ffsll(rest) - 1) >> 2);
-      v = load_group(rows, g, src, ok);
+      ++g;
+      v = load_group(rows, sl, g, src, ok);
     }
     const char* stb = reinterpret_cast<const char*>(sb);
 #pragma unroll
@@ -354,6 +359,7 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
                                            unsigned long long& corner) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4* st4 = reinterpret_cast<float4*>(sm.stage + warp * kStageFloats);
+  unsigned char* sl = sm.slist + warp * kSplitList;
   for (;;) {
     int k = 0;
     if (lane == 0) k = atomicAdd(&X.next, 1);
@@ -366,10 +372,17 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
     const unsigned hi =
         __ballot_sync(kFull, lane + 32 < nc && bit(X.la[lane + 32], ca) && bit(X.lb[lane + 32], cb));
     const unsigned long long m = (unsigned long long)lo | ((unsigned long long)hi << 32);
+    // the pair's live splits in order, then three repeats of the last one
+    const unsigned below = (1u << lane) - 1u;
+    const int nlo = __popc(lo), n = nlo + __popc(hi);
+    if ((lo >> lane) & 1u) sl[__popc(lo & below)] = (unsigned char)lane;
+    if ((hi >> lane) & 1u) sl[nlo + __popc(hi & below)] = (unsigned char)(32 + lane);
+    if (lane < 3) sl[n + lane] = (unsigned char)(hi ? 63 - __clz(hi) : 31 - __clz(lo));
+    __syncwarp();
     const int E = (D.z & 255) * ((D.z >> 8) & 255);
-    if (E <= 128) flat_outer<4>(X, c0, m, D, st4, Mw);
-    else if (E <= 192) flat_outer<6>(X, c0, m, D, st4, Mw);
-    else flat_outer<8>(X, c0, m, D, st4, Mw);
+    if (E <= 128) flat_outer<4>(X, c0, sl, n, D, st4, Mw);
+    else if (E <= 192) flat_outer<6>(X, c0, sl, n, D, st4, Mw);
+    else flat_outer<8>(X, c0, sl, n, D, st4, Mw);
     if (lane == 0) work += (unsigned long long)__popcll(m) * E;
     flat_rules(J, X, D, Mw, P, work, corner);
   }
@@ -736,7 +749,22 @@ __device__ void unary_into(const DevUJob& U, const float* src, float* dst, int c
     const int r0 = __ldg(U.rowptr + t), r1 = __ldg(U.rowptr + t + 1);
     if (r0 == r1) continue;
     float acc = Sr<S>::zero();
-    for (int r = r0; r < r1; ++r) {
+    int r = r0;
+    if (S == SEMI_VITERBI) {
+      // four independent running maxima (max is exact in any order), so four
+      // rule loads are in flight at once
+      float a1 = acc, a2 = acc, a3 = acc;
+      for (; r + 4 <= r1; r += 4) {
+        const int2 q0 = __ldg(U.rules + r), q1 = __ldg(U.rules + r + 1);
+        const int2 q2 = __ldg(U.rules + r + 2), q3 = __ldg(U.rules + r + 3);
+        acc = fmaxf(acc, src[q0.x] + __int_as_float(q0.y));
+        a1 = fmaxf(a1, src[q1.x] + __int_as_float(q1.y));
+        a2 = fmaxf(a2, src[q2.x] + __int_as_float(q2.y));
+        a3 = fmaxf(a3, src[q3.x] + __int_as_float(q3.y));
+      }
+      acc = fmaxf(fmaxf(acc, a1), fmaxf(a2, a3));
+    }
+    for (; r < r1; ++r) {
       const int2 rr = __ldg(U.rules + r);
       acc = Sr<S>::mad(acc, src[rr.x], __int_as_float(rr.y));
     }
@@ -1108,7 +1136,8 @@ size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage) {
   const size_t cs = L.cell_size;
   if (L.mode == 2)
     return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + L.max_mtile)) * sizeof(float) +
-           (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int);
+           (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int) +
+           (with_stage ? (size_t)(kThreads / 32) * kSplitList : 0);
   return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);
 }
 
