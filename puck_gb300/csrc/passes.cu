@@ -170,113 +170,10 @@ __device__ __forceinline__ bool gate_hit(const DevJob& J, int seg, int ms, int m
   return hit;
 }
 
-// Transposed stage of the target-major Viterbi gather: symbol k of split s
-// at st[k * ncp + s]; ncp is nc rounded up to a multiple of four, the extra
-// splits repeating split nc-1 (max is idempotent), so that one 16-byte load
-// reads a symbol's value in four splits.
-__device__ __forceinline__ void stage_transposed(const CellCtx& X, int c0, int nc, int ncp, int cs, float* stA,
-                                                 float* stB) {
-  const int n4 = cs >> 2, per = blockDim.x / ncp;
-  const int s = threadIdx.x % ncp, k0 = threadIdx.x / ncp;
-  if (k0 >= per) return;
-  const float4* ra = reinterpret_cast<const float4*>(X.aptr[c0 + min(s, nc - 1)]);
-  const float4* rb = reinterpret_cast<const float4*>(X.bptr[c0 + min(s, nc - 1)]);
-  for (int k4 = k0; k4 < n4; k4 += per) {
-    const float4 a = __ldg(ra + k4), b = __ldg(rb + k4);
-    float* da = stA + 4 * k4 * ncp + s;
-    float* db = stB + 4 * k4 * ncp + s;
-    da[0] = a.x;
-    da[ncp] = a.y;
-    da[2 * ncp] = a.z;
-    da[3 * ncp] = a.w;
-    db[0] = b.x;
-    db[ncp] = b.y;
-    db[2 * ncp] = b.z;
-    db[3 * ncp] = b.w;
-  }
-}
-
-// Target-major Viterbi gather: the job's rules in CSR order (sorted by
-// target) go in runs of 32, one rule per lane, which warps draw from a
-// shared counter.  A lane folds its rule over the staged splits four at a
-// time (two 16-byte loads, two packed adds, two 3-input maxes), adds the
-// rule weight, and a segmented max over the lanes of each target run leaves
-// one shared-memory atomic max per run.  Exact in any order (max-plus).
-__device__ void gather_targets_viterbi(const DevJob& J, const DevLevel& L, bool gated, float* P, float* stA,
-                                       float* stB, int chunk, CellCtx& X) {
-  const int cs = L.cell_size, ms = L.mask_size;
-  const int lane = threadIdx.x & 31;
-  const int nsp = X.nsp, R = __ldg(J.rowptr + J.n_tgt);
-  unsigned long long work = 0, corner = 0;
-  // targets whose rules run for this cell (segment gated in), one bit each
-  for (int base = 0; base < J.n_tgt; base += blockDim.x) {
-    const int t = base + threadIdx.x;
-    bool ok = false;
-    if (t < J.n_tgt) {
-      const int seg = __ldg(J.tgt_seg + t);
-      ok = seg >= 0 && (!gated || gate_hit(J, seg, ms, L.gate_merged, X.gate));
-    }
-    const unsigned bal = __ballot_sync(kFull, ok);
-    if (lane == 0 && t < J.n_tgt) X.segpass[t >> 5] = bal;
-  }
-  for (int c0 = 0; c0 < nsp; c0 += chunk) {
-    const int nc = min(chunk, nsp - c0), ncp = (nc + 3) & ~3;
-    stage_transposed(X, c0, nc, ncp, cs, stA, stB);
-    if (threadIdx.x == 0) X.next = 0;
-    __syncthreads();
-    for (;;) {
-      int k = 0;
-      if (lane == 0) k = atomicAdd(&X.next, 1);
-      const int r0 = (X.g + __shfl_sync(kFull, k, 0) * X.G) * 32;
-      if (r0 >= R) break;
-      const int r = r0 + lane;
-      const int t = r < R ? __ldg(J.rule_tgt + r) : -1;
-      const bool ok = t >= 0 && ((X.segpass[t >> 5] >> (t & 31)) & 1u);
-      float v = -CUDART_INF_F;
-      if (ok) {
-        const int2 rr = __ldg(J.rules + r);
-        const float4* pa = reinterpret_cast<const float4*>(stA + (rr.x & 0xffff) * ncp);
-        const float4* pb = reinterpret_cast<const float4*>(stB + ((unsigned)rr.x >> 16) * ncp);
-        for (int q = 0; q < (ncp >> 2); ++q) {
-          const float4 a = pa[q], b = pb[q];
-          const float2 t01 = add2(make_float2(a.x, a.y), make_float2(b.x, b.y));
-          const float2 t23 = add2(make_float2(a.z, a.w), make_float2(b.z, b.w));
-          v = max3(v, t01.x, t01.y);
-          v = max3(v, t23.x, t23.y);
-        }
-        v += __int_as_float(rr.y);
-      }
-      // segmented max: lane i ends with the max over lanes i.. of its target run
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const float vo = __shfl_down_sync(kFull, v, o);
-        const int to = __shfl_down_sync(kFull, t, o);
-        if (lane + o < 32 && to == t) v = fmaxf(v, vo);
-      }
-      const int tp = __shfl_up_sync(kFull, t, 1);
-      if (ok && (lane == 0 || tp != t) && v != -CUDART_INF_F) {
-        atomic_fmax(P + t, v);
-        if (v >= 0.f) ++corner;
-      }
-      const unsigned nok = __popc(__ballot_sync(kFull, ok));
-      if (lane == 0) work += (unsigned long long)nok * nc;
-    }
-    __syncthreads();
-  }
-  if (lane == 0 && (work | corner)) {
-    atomicAdd(&X.work, work);
-    atomicAdd(&X.corner, corner);
-  }
-}
-
 // Target-major layout: one warp per target symbol, lanes over its rules.
 template <int S>
 __device__ void gather_targets(const DevJob& J, const DevLevel& L, bool gated, float* P, float* stA, float* stB,
                                int chunk, CellCtx& X) {
-  if (S == SEMI_VITERBI && J.rule_tgt && J.n_tgt <= kMaxSeg && chunk >= 4) {
-    gather_targets_viterbi(J, L, gated, P, stA, stB, chunk, X);
-    return;
-  }
   const int cs = L.cell_size, ms = L.mask_size;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int nsp = X.nsp;
@@ -1015,7 +912,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
 // parents, then the unary layer to outside-bot (and, at span 1, the
 // terminal-child binaries that the reference runs after its span loop).
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4)
+__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
     k_outside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, const float* inside, float* outside, DevLive V,
                    Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
@@ -1250,12 +1147,10 @@ int pick_split_chunk(int cell_size, int max_len) {
   const int static_bytes = (int)sizeof(CellCtx);
   const int budget = (112 * 1024 - static_bytes) / 4;
   int chunk = (budget - 2 * cell_size) / (2 * cell_size);
+  chunk = chunk < 2 ? 2 : chunk;
   chunk = chunk > kMaxSplitChunk ? kMaxSplitChunk : chunk;
   if (max_len > 1 && chunk > max_len) chunk = max_len;
-  // a multiple of four, at least four (the Viterbi gather reads four splits
-  // per load)
-  chunk = (chunk + 3) & ~3;
-  return chunk < 4 ? 4 : chunk;
+  return chunk;
 }
 
 cudaError_t launch_lexicon(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M, float* inside,

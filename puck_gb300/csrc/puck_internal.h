@@ -29,7 +29,6 @@ struct DevJob {
   const int* rowptr;    // [n_tgt + 1]
   const int2* rules;    // [rowptr[n_tgt]]
   const int* tgt_seg;   // [n_tgt] segment of the target's rules, -1 if none
-  const int* rule_tgt;  // [rowptr[n_tgt]] target of each rule (target-major Viterbi levels), or null
   const int* seg_bits;  // [nseg * mask_size] coarse-parent bitset of each segment
   // pair-factored layout (level mode 2): rules grouped by the coarse
   // projection (ca, cb) of their operands ("pairs"), then by segment

@@ -472,14 +472,6 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.rowptr = up<int>(D, L, n + "/rowptr", "i4");
     J.rules = reinterpret_cast<const int2*>(D.upload(packed.data(), packed.size() * sizeof(int2)));
     J.tgt_seg = up<int>(D, L, n + "/tgt_seg", "i4");
-    J.rule_tgt = nullptr;
-    if (L.semiring == puck::SEMI_VITERBI && L.get<int>("in_NN/pair_mode", "i4", nullptr)[0] != 2) {
-      // target-major Viterbi level: the gather takes flat runs of rules
-      std::vector<int> rt(std::max<int64_t>(nab, 1), 0);
-      for (int64_t t = 0; t + 1 < nrow; ++t)
-        for (int r = rowptr_h[t]; r < rowptr_h[t + 1]; ++r) rt[r] = (int)t;
-      J.rule_tgt = static_cast<const int*>(D.upload(rt.data(), rt.size() * sizeof(int)));
-    }
     J.seg_bits = up<int>(D, L, n + "/seg_bits", "i4", &nseg);
     J.nseg = (int)(nseg / std::max(1, L.mask_size));
     if (J.nseg > puck::kMaxSeg) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "more than 2048 rule segments in " + n};
