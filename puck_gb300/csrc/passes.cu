@@ -911,8 +911,12 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
 // Outside pass over the cells of a work list: outside-top of each cell gathered from its
 // parents, then the unary layer to outside-bot (and, at span 1, the
 // terminal-child binaries that the reference runs after its span loop).
+// Register budgets: five CTAs per SM for the pair-factored passes, six for
+// the target-major Viterbi pass (40 registers; 15% faster than four CTAs at
+// 64 on the bench's coarse level despite a few spilled bytes), four for the
+// target-major sum-product passes.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 4)
+__global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4)
     k_outside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, const float* inside, float* outside, DevLive V,
                    Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
