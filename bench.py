@@ -45,7 +45,7 @@ sys.path.insert(0, ROOT)
 
 N_SENT = 20000
 MAX_LEN = 40
-FINE_INSIDE_BYTES_PER_UNIT = 0.0893
+FINE_INSIDE_BYTES_PER_UNIT = 0.0813
 
 
 def log(*a):
