@@ -236,7 +236,7 @@ __device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned lon
 }
 
 // This lane's operand value for each of the four splits of group g (see
-// flat_outer): one 4-byte load fetches the group's split positions from the
+// grid_outer): one 4-byte load fetches the group's split positions from the
 // warp's live-split list, then their row pointers.
 __device__ __forceinline__ float4 load_group(const float* const* rows, const unsigned char* sl, int g, unsigned src,
                                              bool ok) {
@@ -249,43 +249,35 @@ __device__ __forceinline__ float4 load_group(const float* const* rows, const uns
   return v;
 }
 
-// Outer product of one pair in the flat-tile layout (DevJob::pair_desc): lane
-// slot i holds tile entry e = lane + 32 * i = j * nz + k, i < NS, and ends
-// with max over the pair's live splits s of fl(A_s[Y_j] + B_s[Z_k]), which
-// it stores to the warp's M tile.  The n live splits (the warp's list sl,
-// padded by repeats of the last one: max is idempotent) go in groups of
-// four.  Per group, lanes 0-15 stage the A members of the four splits as one float4 row
-// each, lanes 16-31 the B members; each slot then reads its two rows (one
-// 16-byte load each) and folds four sums into its entry with two packed adds
-// and two 3-input maxes.  The operand loads of the next live group are
-// issued before the current group's arithmetic, into the other of the warp's
-// two stage buffers.  Slots past the tile read the -inf rows and are not
-// stored.
-template <int NS>
-__device__ __forceinline__ void flat_outer(const CellCtx& X, int c0, const unsigned char* sl, int n, int4 D,
+// Outer product of one pair in the flat-tile layout (DevJob::pair_desc) into
+// the warp's M tile: M[j * nz + k] = max over the pair's live splits s of
+// fl(A_s[Y_j] + B_s[Z_k]).  The lanes form an 8 x 4 grid: lane (jg, kg) =
+// (lane / 4, lane % 4) holds the RJ x RK entries j = jg + 8a, k = kg + 4b, so
+// that each A row it reads serves RK entries and each B row RJ entries.  The
+// n live splits (the warp's list sl, padded by repeats of the last one: max
+// is idempotent) go in groups of four.  Per group, lanes 0-15 stage the A
+// members of the four splits as one float4 row each, lanes 16-31 the B
+// members; a lane then reads its RJ A rows and RK B rows (one 16-byte load
+// each) and folds four sums into each entry with two packed adds and two
+// 3-input maxes.  The operand loads of the next group are issued before the
+// current group's arithmetic, into the other of the warp's two stage buffers.
+// Rows past the tile read the -inf rows; their entries are not stored.
+template <int RJ, int RK>
+__device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsigned char* sl, int n, int4 D,
                                            float4* st4, float* Mw) {
   const int lane = threadIdx.x & 31;
-  const int ny = D.z & 255, nz = (D.z >> 8) & 255, E = ny * nz;
-  // j = lane / nz, k = lane % nz; then 32 entries further per slot.  The
-  // float quotient is exact here: (lane + 1/2) / nz is at least 1/32 away
-  // from an integer, far beyond the rounding of the product.
-  const float inv = __frcp_rn((float)nz);
-  int j = (int)(((float)lane + 0.5f) * inv), k = lane - j * nz;
-  const int dq = (int)(32.5f * inv), dr = 32 - dq * nz;
-  unsigned off[NS];  // byte offsets of the slot's A row | B row << 16 (buffer 0)
-  float acc[NS];
+  const int ny = D.z & 255, nz = (D.z >> 8) & 255;
+  const int jg = lane >> 2, kg = lane & 3;
+  unsigned offA[RJ], offB[RK];  // byte offsets of the lane's rows in buffer 0
 #pragma unroll
-  for (int i = 0; i < NS; ++i) {
-    const bool in = lane + 32 * i < E;
-    off[i] = (unsigned)((in ? j : 16) * 16) | (unsigned)((kStageRowB + (in ? k : 16)) * 16) << 16;
-    acc[i] = -CUDART_INF_F;
-    j += dq;
-    k += dr;
-    if (k >= nz) {
-      k -= nz;
-      ++j;
-    }
-  }
+  for (int a = 0; a < RJ; ++a) offA[a] = (unsigned)((jg + 8 * a < ny ? jg + 8 * a : 16) * 16);
+#pragma unroll
+  for (int b = 0; b < RK; ++b) offB[b] = (unsigned)((kStageRowB + (kg + 4 * b < nz ? kg + 4 * b : 16)) * 16);
+  float acc[RJ][RK];
+#pragma unroll
+  for (int a = 0; a < RJ; ++a)
+#pragma unroll
+    for (int b = 0; b < RK; ++b) acc[a][b] = -CUDART_INF_F;
   const bool a_side = lane < 16;
   const int mem = a_side ? lane : lane - 16;
   const bool ok = mem < (a_side ? ny : nz);
@@ -304,20 +296,27 @@ __device__ __forceinline__ void flat_outer(const CellCtx& X, int c0, const unsig
       v = load_group(rows, sl, g, src, ok);
     }
     const char* stb = reinterpret_cast<const char*>(sb);
+    float4 A[RJ];
 #pragma unroll
-    for (int i = 0; i < NS; ++i) {
-      const float4 a = *reinterpret_cast<const float4*>(stb + (off[i] & 0xffffu));
-      const float4 b = *reinterpret_cast<const float4*>(stb + (off[i] >> 16));
-      const float2 t01 = add2(make_float2(a.x, a.y), make_float2(b.x, b.y));
-      const float2 t23 = add2(make_float2(a.z, a.w), make_float2(b.z, b.w));
-      acc[i] = max3(acc[i], t01.x, t01.y);
-      acc[i] = max3(acc[i], t23.x, t23.y);
+    for (int a = 0; a < RJ; ++a) A[a] = *reinterpret_cast<const float4*>(stb + offA[a]);
+#pragma unroll
+    for (int b = 0; b < RK; ++b) {
+      const float4 B = *reinterpret_cast<const float4*>(stb + offB[b]);
+#pragma unroll
+      for (int a = 0; a < RJ; ++a) {
+        const float2 t01 = add2(make_float2(A[a].x, A[a].y), make_float2(B.x, B.y));
+        const float2 t23 = add2(make_float2(A[a].z, A[a].w), make_float2(B.z, B.w));
+        acc[a][b] = max3(acc[a][b], t01.x, t01.y);
+        acc[a][b] = max3(acc[a][b], t23.x, t23.y);
+      }
     }
     if (!rest) break;
   }
 #pragma unroll
-  for (int i = 0; i < NS; ++i)
-    if (lane + 32 * i < E) Mw[lane + 32 * i] = acc[i];
+  for (int a = 0; a < RJ; ++a)
+#pragma unroll
+    for (int b = 0; b < RK; ++b)
+      if (jg + 8 * a < ny && kg + 4 * b < nz) Mw[(jg + 8 * a) * nz + kg + 4 * b] = acc[a][b];
   __syncwarp();
 }
 
@@ -379,10 +378,16 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
     if ((hi >> lane) & 1u) sl[nlo + __popc(hi & below)] = (unsigned char)(32 + lane);
     if (lane < 3) sl[n + lane] = (unsigned char)(hi ? 63 - __clz(hi) : 31 - __clz(lo));
     __syncwarp();
-    const int E = (D.z & 255) * ((D.z >> 8) & 255);
-    if (E <= 128) flat_outer<4>(X, c0, sl, n, D, st4, Mw);
-    else if (E <= 192) flat_outer<6>(X, c0, sl, n, D, st4, Mw);
-    else flat_outer<8>(X, c0, sl, n, D, st4, Mw);
+    const int ny = D.z & 255, nz = (D.z >> 8) & 255, E = ny * nz;
+    const int shape = (ny > 8 ? 3 : 0) + (nz > 12 ? 2 : nz > 8 ? 1 : 0);  // RJ in {1, 2} x RK in {2, 3, 4}
+    switch (shape) {
+      case 0: grid_outer<1, 2>(X, c0, sl, n, D, st4, Mw); break;
+      case 1: grid_outer<1, 3>(X, c0, sl, n, D, st4, Mw); break;
+      case 2: grid_outer<1, 4>(X, c0, sl, n, D, st4, Mw); break;
+      case 3: grid_outer<2, 2>(X, c0, sl, n, D, st4, Mw); break;
+      case 4: grid_outer<2, 3>(X, c0, sl, n, D, st4, Mw); break;
+      default: grid_outer<2, 4>(X, c0, sl, n, D, st4, Mw); break;
+    }
     if (lane == 0) work += (unsigned long long)__popcll(m) * E;
     flat_rules(J, X, D, Mw, P, work, corner);
   }
