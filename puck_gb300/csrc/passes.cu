@@ -393,8 +393,10 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
   }
 }
 
-// Pair-factored gather (level mode 2), see the file comment.
-template <int S>
+// Pair-factored gather (level mode 2), see the file comment.  FLAT: every
+// job this kernel runs is in the flat-tile form, so the other pair loops are
+// not compiled in (a smaller kernel for the instruction cache).
+template <int S, bool FLAT = false>
 __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
                              CellCtx& X) {
   const int ms = L.mask_size, nco = L.n_coarse;
@@ -484,11 +486,12 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
     const int nlive = X.nlive;
-    if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage) {
+    if (FLAT || (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage)) {
       flat_pairs(J, sm, X, c0, nc, nlive, Mw, P, work, corner);
       __syncthreads();
       continue;
     }
+    if (FLAT) continue;  // not reached
     for (int i = X.g * nwarps + warp; i < nlive; i += X.G * nwarps) {
       const int p = sm.list[i];
       const int key = __ldg(J.pair_key + p);
@@ -714,10 +717,13 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
   }
 }
 
+// MODE 0 target-major, 2 pair-factored, 3 pair-factored with every job in
+// the flat-tile form (Viterbi inside passes).
 template <int S, int MODE>
 __device__ __forceinline__ void gather(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
                                        int chunk, CellCtx& X) {
-  if (MODE == 2 && S != SEMI_LOGSUM) gather_pairs<S>(J, L, gated, P, sm, X);
+  if (MODE == 3) gather_pairs<S, true>(J, L, gated, P, sm, X);
+  else if (MODE == 2 && S != SEMI_LOGSUM) gather_pairs<S>(J, L, gated, P, sm, X);
   else gather_targets<S>(J, L, gated, P, sm.stA, sm.stB, chunk, X);
 }
 
@@ -821,7 +827,7 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 // passes (48 registers: the flat-tile path keeps up to eight tile entries
 // and their stage offsets in registers), six for the target-major ones.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE == 2 ? 5 : 6)
+__global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
     k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
@@ -1187,7 +1193,7 @@ cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, 
   if (inside_pass) {
     if (cudaError_t e = set_smem(k_inside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_inside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside, V, C, chunk);
-  } else {
+  } else if (MODE != 3) {
     if (cudaError_t e = set_smem(k_outside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_outside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside_c, outside, V, C, chunk);
   }
@@ -1201,6 +1207,8 @@ cudaError_t launch_any(bool inside_pass, const DevLevel& L, const DevBatch& B, c
   const bool pairs = L.mode == 2;
   switch (L.semiring) {
     case SEMI_VITERBI:
+      if (pairs && inside_pass && L.flat_inside)
+        return launch_pass<SEMI_VITERBI, 3>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
       return pairs ? launch_pass<SEMI_VITERBI, 2>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st)
                    : launch_pass<SEMI_VITERBI, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
     case SEMI_REAL:

@@ -77,6 +77,7 @@ struct DevLevel {
   int max_npair;    // largest pair count of any job (shared-memory list size)
   int max_mtile;    // largest ny * nz of any pair (per-warp outer-product tile)
   int tc_binary;    // sum-product inside pass: binary sums already in the bot cells (tensor-core form)
+  int flat_inside;  // every inside job with rules is in the flat-tile form (DevJob::interleaved == 3)
   const int* nt_mem_off;  // [n_coarse + 1] coarse -> nonterminal members
   const int* nt_mem;
   const int* t_mem_off;   // [n_coarse + 1] coarse -> terminal members

@@ -639,6 +639,9 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
       d.max_mtile = std::max(d.max_mtile, (ao[ca + 1] - ao[ca]) * (bo[cb + 1] - bo[cb]));
     }
   }
+  d.flat_inside = 1;
+  for (int j = puck::IN_NN; j <= puck::IN_TT; ++j)
+    if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0 && d.jobs[j].interleaved != 3) d.flat_inside = 0;
   {
     const int* nn_mode = L.get<int>("in_NN/pair_mode", "i4", nullptr);
     d.mode = (nn_mode[0] == 2 && L.semiring != puck::SEMI_LOGSUM) ? 2 : 0;
