@@ -164,7 +164,8 @@ puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[
  * keeps, for the whole parser, how many waves of CTAs the cells of a span
  * launch that does not fill the GPU are split to fill (1, 2 or 4).  chosen
  * (levels + 1 entries, may be NULL) receives each level's gather form (0
- * target-major, 2 pair-factored; the archive's choice) and the waves x 100.
+ * target-major, 2 pair-factored, 3 pair-factored with the flat-tile inside
+ * pass; the archive's choice) and the waves x 100.
  * Results do not depend on the choice (Viterbi bit-identical; Real sums
  * reorder). */
 puck_status puck_parser_autotune(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,

@@ -81,7 +81,15 @@ struct Smem {
   unsigned* pl;
   int* list;
   unsigned char* slist;  // per warp kSplitList: the live splits of the warp's current pair (flat-tile path)
+  int mtile;             // floats of each warp's M tile
 };
+
+// Floats of each warp's outer-product tile: the flat-tile sub-tiles (at most
+// 16 x 16) in the Viterbi inside kernel of a level whose inside jobs are all
+// flat, else the level's largest pair.
+__host__ __device__ __forceinline__ int mtile_floats(const DevLevel& L, bool with_stage) {
+  return with_stage && L.flat_inside ? L.flat_mtile : L.max_mtile;
+}
 
 // with_stage: the per-warp operand stage of the Viterbi inside pass
 __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage) {
@@ -94,13 +102,14 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
   m.pl = nullptr;
   m.list = nullptr;
   m.slist = nullptr;
+  m.mtile = mtile_floats(L, with_stage);
   if (L.mode == 2) {
     if (with_stage) {
       m.stage = rest;
       rest += (blockDim.x >> 5) * kStageFloats;
     }
     m.M = rest;
-    m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * L.max_mtile);
+    m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * m.mtile);
     m.list = reinterpret_cast<int*>(m.pl + L.n_coarse * L.mask_size);
     if (with_stage) m.slist = reinterpret_cast<unsigned char*>(m.list + L.max_npair);
   } else {
@@ -405,7 +414,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
   const int* amem = J.a_is_t ? L.t_mem : L.nt_mem;
   const int* boff = J.b_is_t ? L.t_mem_off : L.nt_mem_off;
   const int* bmem = J.b_is_t ? L.t_mem : L.nt_mem;
-  float* Mw = sm.M + warp * L.max_mtile;
+  float* Mw = sm.M + warp * sm.mtile;
   const int nsp = X.nsp;
   unsigned long long work = 0, corner = 0;
   if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage && threadIdx.x < 4 && nsp > 0) {
@@ -1150,7 +1159,8 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage) {
   const size_t cs = L.cell_size;
   if (L.mode == 2)
-    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + L.max_mtile)) * sizeof(float) +
+    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + mtile_floats(L, with_stage))) *
+               sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int) +
            (with_stage ? (size_t)(kThreads / 32) * kSplitList : 0);
   return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);

@@ -78,6 +78,8 @@ struct DevLevel {
   int max_mtile;    // largest ny * nz of any pair (per-warp outer-product tile)
   int tc_binary;    // sum-product inside pass: binary sums already in the bot cells (tensor-core form)
   int flat_inside;  // every inside job with rules is in the flat-tile form (DevJob::interleaved == 3)
+  int flat_mtile;   // largest ny * nz of any flat-tile sub-tile (<= 256); the M tile of the
+                    // Viterbi inside kernel when flat_inside
   const int* nt_mem_off;  // [n_coarse + 1] coarse -> nonterminal members
   const int* nt_mem;
   const int* t_mem_off;   // [n_coarse + 1] coarse -> terminal members

@@ -295,17 +295,25 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
   return reinterpret_cast<const T*>(D.upload(h, c * sizeof(T)));
 }
 
-// The flat-tile layout of a Viterbi inside job (DevJob::pair_desc, fr_*):
-// built when every pair's operand members are contiguous index ranges of at
-// most 16 symbols per side and every block has at most 32 targets.  Each
-// target of a block gets lanes in proportion to its rule count (at least
-// one); a lane's slice is stored as records of four rules, padded with
-// weight -inf (the max-plus zero, which never changes a cell).
-// Returns false, uploading nothing, when the job does not qualify.
+// The flat-tile layout of a Viterbi inside job (DevJob::pair_desc, fr_*),
+// built when every pair's operand members are contiguous index ranges.  A
+// pair whose coarse symbols have more than 16 members on a side is cut into
+// sub-tiles of at most 16 x 16 (16 members, then the rest): each sub-tile is
+// a pair of its own, with the same coarse key (its liveness test), the rules
+// whose two operands fall inside it and the OR of its blocks' segment bits
+// as its gate.  A block with more than 32 targets is cut into runs of 32
+// targets.  Each target of a block gets lanes in proportion to its rule
+// count (at least one); a lane's slice is stored as records of four rules,
+// padded with weight -inf (the max-plus zero, which never changes a cell).
+// The job's pair list (npair, pair_key, pair_gate) becomes the sub-tile
+// list.  *mtile receives the largest sub-tile.  Returns false, uploading
+// nothing, when the job does not qualify.
 bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int ntgt, int64_t npk,
-                      const int* pk, const int* pbk, const int* bs, const int* bp, const int* pr, const float* pw) {
+                      const int* pk, const int* pbk, const int* bs, const int* bp, const int* pr, const float* pw,
+                      const int* seg_bits, int nseg, int ms, int* mtile) {
   static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
   static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
+  constexpr int kSub = 16;  // largest sub-tile side
   const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
   const int* am = L.get<int>(a_t[j] ? "t_mem" : "nt_mem", "i4", nullptr);
   const int* bo = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
@@ -315,127 +323,179 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, i
       if (mem[i] != mem[off[c]] + (i - off[c])) return false;
     return true;
   };
-  std::vector<int4> desc(std::max<int64_t>(npk, 1));
+  struct FlatRule {
+    int t, e;
+    float w;
+  };
+  std::vector<int4> desc, blk;
+  std::vector<int> key, gate, tgt;
+  std::vector<unsigned> idx;
+  std::vector<float4> w;
+  int max_tile = 1;
+  // One block of a sub-tile: rules sorted by target, at most 32 targets.
+  auto emit_block = [&](int seg, const std::vector<FlatRule>& rs, int tile) -> bool {
+    const int cnt = (int)rs.size();
+    const size_t b = blk.size();
+    tgt.resize((b + 1) * 32, -1);
+    std::vector<int> tstart, tcnt, tlanes;
+    for (int r = 0; r < cnt; ++r)
+      if (r == 0 || rs[r].t != rs[r - 1].t) tstart.push_back(r);
+    if (tstart.size() > 32) return false;
+    for (size_t t = 0; t < tstart.size(); ++t) tcnt.push_back((t + 1 < tstart.size() ? tstart[t + 1] : cnt) - tstart[t]);
+    tlanes.assign(tstart.size(), 1);
+    auto slice = [&](size_t t) { return (tcnt[t] + tlanes[t] - 1) / tlanes[t]; };
+    for (int free_lanes = 32 - (int)tstart.size(); free_lanes > 0 && !tstart.empty(); --free_lanes) {
+      size_t best = 0;
+      for (size_t t = 1; t < tstart.size(); ++t)
+        if (slice(t) > slice(best)) best = t;
+      if (slice(best) <= 1) break;
+      ++tlanes[best];
+    }
+    int per = 0;
+    for (size_t t = 0; t < tstart.size(); ++t) per = std::max(per, slice(t));
+    const int steps = (per + 3) / 4, slots = 4 * steps;
+    // each lane's rules (tile entry, weight), in any order: max is commutative
+    std::vector<std::vector<std::pair<int, float>>> todo(32);
+    int lane = 0;
+    for (size_t t = 0; t < tstart.size(); ++t) {
+      const int len = slice(t);
+      for (int l = 0; l < tlanes[t]; ++l, ++lane) {
+        const int a0 = tstart[t] + l * len, a1 = std::min(tstart[t] + tcnt[t], a0 + len);
+        tgt[b * 32 + lane] = rs[tstart[t]].t;
+        for (int r = a0; r < a1; ++r) todo[lane].push_back({rs[r].e, rs[r].w});
+      }
+    }
+    // Each slot (one of the four loads of a record) is one warp-wide shared
+    // load of M: its 32 tile entries should fall in distinct banks (e mod
+    // 32), or read the same entry.  Slot by slot, lanes that must take a
+    // rule now (as many rules left as slots) pick first; the others take a
+    // rule only in a bank still free.  A lane without a rule this slot
+    // reads an entry already read by the slot (weight -inf).
+    const size_t base = idx.size();
+    idx.resize(base + (size_t)steps * 32, 0u);
+    w.resize(base + (size_t)steps * 32, make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
+    for (int sl = 0; sl < slots; ++sl) {
+      int bank_e[32];
+      std::fill(bank_e, bank_e + 32, -1);
+      int pick[32];
+      std::fill(pick, pick + 32, -1);
+      auto choose = [&](int l, bool forced) {
+        auto& v = todo[l];
+        int best = -1;
+        for (size_t r = 0; r < v.size(); ++r) {
+          const int e = v[r].first, bk = e & 31;
+          if (bank_e[bk] < 0 || bank_e[bk] == e) {
+            best = (int)r;
+            break;
+          }
+        }
+        if (best < 0 && forced) best = 0;
+        if (best < 0) return;
+        pick[l] = best;
+        const int e = v[best].first;
+        if (bank_e[e & 31] < 0) bank_e[e & 31] = e;
+      };
+      for (int l = 0; l < 32; ++l)
+        if (!todo[l].empty() && (int)todo[l].size() >= slots - sl) choose(l, true);
+      for (int l = 0; l < 32; ++l)
+        if (pick[l] < 0 && !todo[l].empty() && (int)todo[l].size() < slots - sl) choose(l, false);
+      int any_e = 0;
+      for (int k = 0; k < 32; ++k)
+        if (bank_e[k] >= 0) {
+          any_e = bank_e[k];
+          break;
+        }
+      for (int l = 0; l < 32; ++l) {
+        const size_t at = base + (size_t)(sl / 4) * 32 + l;
+        int e = any_e;
+        float wt = -INFINITY;
+        if (pick[l] >= 0) {
+          e = todo[l][pick[l]].first;
+          wt = todo[l][pick[l]].second;
+          todo[l].erase(todo[l].begin() + pick[l]);
+        }
+        idx[at] |= (unsigned)e << (8 * (sl % 4));
+        (&w[at].x)[sl % 4] = wt;
+      }
+    }
+    for (int l = 0; l < 32; ++l)
+      if (!todo[l].empty()) return false;  // cannot happen: every lane has slots for all its rules
+    // every tile entry inside the sub-tile (a byte each), every target below
+    // the job's target count
+    for (size_t q = base; q < idx.size(); ++q)
+      for (int c = 0; c < 4; ++c)
+        if ((int)((idx[q] >> (8 * c)) & 255u) >= tile) return false;
+    for (int l = 0; l < 32; ++l)
+      if (tgt[b * 32 + l] >= ntgt) return false;
+    if (idx.size() > (size_t)INT32_MAX) return false;
+    blk.push_back(make_int4(seg, (int)base, (int)idx.size(), cnt));
+    return true;
+  };
+  std::vector<FlatRule> rs;
+  std::vector<unsigned> g(std::max(ms, 1));
   for (int64_t k = 0; k < npk; ++k) {
     const int ca = pk[k] & 255, cb = (pk[k] >> 8) & 255;
     const int ny = ao[ca + 1] - ao[ca], nz = bo[cb + 1] - bo[cb];
-    if (ny < 1 || nz < 1 || ny > 16 || nz > 16 || !contiguous(ao, am, ca) || !contiguous(bo, bm, cb)) return false;
-    if (pbk[k + 1] - pbk[k] > 65535) return false;
-    desc[k] = make_int4(am[ao[ca]] | bm[bo[cb]] << 16, pbk[k], ny | nz << 8 | (pbk[k + 1] - pbk[k]) << 16,
-                        ca | cb << 8);
-  }
-  const int nblk = npk > 0 ? pbk[npk] : 0;
-  std::vector<int> tgt((size_t)std::max(nblk, 1) * 32, -1);
-  std::vector<int4> blk((size_t)std::max(nblk, 1), make_int4(0, 0, 0, 0));
-  std::vector<unsigned> idx;
-  std::vector<float4> w;
-  for (int64_t k = 0; k < npk; ++k) {
-    const int ny = desc[k].z & 255, nz = (desc[k].z >> 8) & 255;
-    for (int b = pbk[k]; b < pbk[k + 1]; ++b) {
-      const int r0 = bp[b], cnt = bp[b + 1] - bp[b];
-      // targets of the block (its rules are sorted by target) and their lanes
-      std::vector<int> tstart, tcnt, tlanes;
-      for (int r = 0; r < cnt; ++r)
-        if (r == 0 || ((unsigned)pr[r0 + r] >> 16) != ((unsigned)pr[r0 + r - 1] >> 16)) tstart.push_back(r);
-      if (tstart.size() > 32) return false;
-      for (size_t t = 0; t < tstart.size(); ++t) tcnt.push_back((t + 1 < tstart.size() ? tstart[t + 1] : cnt) - tstart[t]);
-      tlanes.assign(tstart.size(), 1);
-      auto slice = [&](size_t t) { return (tcnt[t] + tlanes[t] - 1) / tlanes[t]; };
-      for (int free_lanes = 32 - (int)tstart.size(); free_lanes > 0 && !tstart.empty(); --free_lanes) {
-        size_t best = 0;
-        for (size_t t = 1; t < tstart.size(); ++t)
-          if (slice(t) > slice(best)) best = t;
-        if (slice(best) <= 1) break;
-        ++tlanes[best];
-      }
-      int per = 0;
-      for (size_t t = 0; t < tstart.size(); ++t) per = std::max(per, slice(t));
-      const int steps = (per + 3) / 4, slots = 4 * steps;
-      // each lane's rules (tile entry, weight), in any order: max is commutative
-      std::vector<std::vector<std::pair<int, float>>> todo(32);
-      int lane = 0;
-      for (size_t t = 0; t < tstart.size(); ++t) {
-        const int len = slice(t);
-        for (int l = 0; l < tlanes[t]; ++l, ++lane) {
-          const int a0 = tstart[t] + l * len, a1 = std::min(tstart[t] + tcnt[t], a0 + len);
-          tgt[(size_t)b * 32 + lane] = (int)((unsigned)pr[r0 + tstart[t]] >> 16);
-          for (int r = a0; r < a1; ++r) {
-            const int x = pr[r0 + r];
-            todo[lane].push_back({(x & 255) * nz + ((x >> 8) & 255), pw[r0 + r]});
+    if (ny < 1 || nz < 1 || ny > 255 || nz > 255 || !contiguous(ao, am, ca) || !contiguous(bo, bm, cb)) return false;
+    for (int y0 = 0; y0 < ny; y0 += kSub)
+      for (int z0 = 0; z0 < nz; z0 += kSub) {
+        const int sy = std::min(kSub, ny - y0), sz = std::min(kSub, nz - z0);
+        const int a_first = am[ao[ca]] + y0, b_first = bm[bo[cb]] + z0;
+        if (a_first > 0xffff || b_first > 0xffff) return false;
+        const int b_first_blk = (int)blk.size();
+        std::fill(g.begin(), g.end(), 0u);
+        for (int b = pbk[k]; b < pbk[k + 1]; ++b) {
+          if (bs[b] < 0 || bs[b] >= nseg) return false;
+          // the block's rules inside this sub-tile, in target order
+          rs.clear();
+          for (int r = bp[b]; r < bp[b + 1]; ++r) {
+            const unsigned x = (unsigned)pr[r];
+            const int jj = (int)(x & 255u) - y0, kk = (int)((x >> 8) & 255u) - z0;
+            if (jj >= 0 && jj < sy && kk >= 0 && kk < sz) rs.push_back({(int)(x >> 16), jj * sz + kk, pw[r]});
           }
-        }
-      }
-      // Each slot (one of the four loads of a record) is one warp-wide shared
-      // load of M: its 32 tile entries should fall in distinct banks (e mod
-      // 32), or read the same entry.  Slot by slot, lanes that must take a
-      // rule now (as many rules left as slots) pick first; the others take a
-      // rule only in a bank still free.  A lane without a rule this slot
-      // reads an entry already read by the slot (weight -inf).
-      const size_t base = idx.size();
-      idx.resize(base + (size_t)steps * 32, 0u);
-      w.resize(base + (size_t)steps * 32, make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
-      for (int sl = 0; sl < slots; ++sl) {
-        int bank_e[32];
-        std::fill(bank_e, bank_e + 32, -1);
-        int pick[32];
-        std::fill(pick, pick + 32, -1);
-        auto choose = [&](int l, bool forced) {
-          auto& v = todo[l];
-          int best = -1;
-          for (size_t r = 0; r < v.size(); ++r) {
-            const int e = v[r].first, bk = e & 31;
-            if (bank_e[bk] < 0 || bank_e[bk] == e) {
-              best = (int)r;
-              break;
+          if (rs.empty()) continue;
+          for (int i = 0; i < ms; ++i) g[i] |= (unsigned)seg_bits[(size_t)bs[b] * ms + i];
+          // runs of at most 32 targets
+          size_t r0 = 0;
+          while (r0 < rs.size()) {
+            size_t r1 = r0;
+            int ntg = 0;
+            while (r1 < rs.size() && (ntg < 32 || rs[r1].t == rs[r1 - 1].t)) {
+              if (r1 == r0 || rs[r1].t != rs[r1 - 1].t) ++ntg;
+              ++r1;
             }
+            if (!emit_block(bs[b], std::vector<FlatRule>(rs.begin() + r0, rs.begin() + r1), sy * sz)) return false;
+            r0 = r1;
           }
-          if (best < 0 && forced) best = 0;
-          if (best < 0) return;
-          pick[l] = best;
-          const int e = v[best].first;
-          if (bank_e[e & 31] < 0) bank_e[e & 31] = e;
-        };
-        for (int l = 0; l < 32; ++l)
-          if (!todo[l].empty() && (int)todo[l].size() >= slots - sl) choose(l, true);
-        for (int l = 0; l < 32; ++l)
-          if (pick[l] < 0 && !todo[l].empty() && (int)todo[l].size() < slots - sl) choose(l, false);
-        int any_e = 0;
-        for (int k = 0; k < 32; ++k)
-          if (bank_e[k] >= 0) {
-            any_e = bank_e[k];
-            break;
-          }
-        for (int l = 0; l < 32; ++l) {
-          const size_t at = base + (size_t)(sl / 4) * 32 + l;
-          int e = any_e;
-          float wt = -INFINITY;
-          if (pick[l] >= 0) {
-            e = todo[l][pick[l]].first;
-            wt = todo[l][pick[l]].second;
-            todo[l].erase(todo[l].begin() + pick[l]);
-          }
-          idx[at] |= (unsigned)e << (8 * (sl % 4));
-          (&w[at].x)[sl % 4] = wt;
         }
+        const int nb = (int)blk.size() - b_first_blk;
+        if (nb == 0) continue;
+        if (nb > 0xffff) return false;
+        desc.push_back(make_int4(a_first | b_first << 16, b_first_blk, sy | sz << 8 | nb << 16, ca | cb << 8));
+        key.push_back(ca | cb << 8);
+        for (int i = 0; i < ms; ++i) gate.push_back((int)g[i]);
+        max_tile = std::max(max_tile, sy * sz);
       }
-      for (int l = 0; l < 32; ++l)
-        if (!todo[l].empty()) return false;  // cannot happen: every lane has slots for all its rules
-      // every tile entry inside the pair's tile (a byte each), every target
-      // below the job's target count
-      for (size_t q = base; q < idx.size(); ++q)
-        for (int c = 0; c < 4; ++c)
-          if ((int)((idx[q] >> (8 * c)) & 255u) >= ny * nz) return false;
-      for (int l = 0; l < 32; ++l)
-        if (tgt[(size_t)b * 32 + l] >= ntgt) return false;
-      if (idx.size() > (size_t)INT32_MAX) return false;
-      blk[b] = make_int4(bs[b], (int)base, (int)idx.size(), cnt);
-    }
   }
+  if (desc.size() > (size_t)INT32_MAX / 32) return false;
+  J.npair = (int)desc.size();
+  if (desc.empty()) desc.push_back(make_int4(0, 0, 0, 0));  // a job without rules still gets (never read) tables
+  if (key.empty()) key.push_back(0);
+  if (gate.empty()) gate.assign(std::max(ms, 1), 0);
+  if (blk.empty()) blk.push_back(make_int4(0, 0, 0, 0));
+  if (tgt.empty()) tgt.assign(32, -1);
+  if (idx.empty()) {
+    idx.push_back(0u);
+    w.push_back(make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
+  }
+  J.pair_key = static_cast<const int*>(D.upload(key.data(), key.size() * sizeof(int)));
+  J.pair_gate = static_cast<const int*>(D.upload(gate.data(), gate.size() * sizeof(int)));
   J.pair_desc = static_cast<const int4*>(D.upload(desc.data(), desc.size() * sizeof(int4)));
   J.fr_blk = static_cast<const int4*>(D.upload(blk.data(), blk.size() * sizeof(int4)));
   J.fr_tgt = static_cast<const int*>(D.upload(tgt.data(), tgt.size() * sizeof(int)));
   J.fr_idx = static_cast<const unsigned*>(D.upload(idx.data(), idx.size() * sizeof(unsigned)));
   J.fr_w = static_cast<const float4*>(D.upload(w.data(), w.size() * sizeof(float4)));
+  *mtile = std::max(*mtile, max_tile);
   return true;
 }
 
@@ -618,13 +678,16 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     if (rr.size() > (size_t)INT32_MAX) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "pair rule table too large in " + n};
     J.npair = (int)npk;
     J.interleaved = !interleave ? 0 : one_target_lanes ? 2 : 1;
-    if (J.interleaved == 2 &&
-        build_flat_tiles(D, J, L, j, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw))
-      J.interleaved = 3;
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
     J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
+    // Viterbi inside jobs take the flat-tile form where it applies (it
+    // replaces the pair list by its sub-tile list)
+    if (interleave && build_flat_tiles(D, J, L, j, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr),
+                                       bp, pr, pw, L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size,
+                                       &d.flat_mtile))
+      J.interleaved = 3;
     J.pair_blk = up<int>(D, L, n + "/pair_blk", "i4");
     J.blk_seg = up<int>(D, L, n + "/blk_seg", "i4");
     J.blk_ptr = static_cast<const int*>(D.upload(dev_bp.data(), dev_bp.size() * sizeof(int)));
@@ -1601,7 +1664,8 @@ puck_status puck_parser_autotune(puck_parser* P, const int32_t* word_ids, const 
   }
   P->waves = best_w;
   if (chosen) {
-    for (int l = 0; l < nl; ++l) chosen[l] = P->tuned_mode[l];
+    for (int l = 0; l < nl; ++l)
+      chosen[l] = P->tuned_mode[l] == 2 && P->levels[l]->d.flat_inside ? 3 : P->tuned_mode[l];
     chosen[nl] = (int32_t)(best_w * 100);
   }
   return PUCK_OK;

@@ -323,7 +323,7 @@ class CLParser:
         nl = len(self.data)
         out = np.zeros(nl + 1, np.int32)
         _lib.check(self._L.puck_parser_autotune(self._p, _ptr(words), _ptr(offsets), len(offsets) - 1, _ptr(out)))
-        names = {0: "target-major", 2: "pair-factored"}
+        names = {0: "target-major", 2: "pair-factored", 3: "pair-factored, flat-tile inside"}
         return {"levels": [names.get(int(m), str(int(m))) for m in out[:nl]], "waves": int(out[nl]) / 100.0}
 
     def tensor_cores(self, level: int):

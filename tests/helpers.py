@@ -40,6 +40,12 @@ def split_levels(fine_semiring="viterbi", size="medium"):
         # each path of the fine kernel (<= 16 members, <= 32, and larger tiles)
         c, f = synth.split_grammar(seed=11, n_coarse_nt=8, n_coarse_pt=6, max_split=30, mean_split=13.0,
                                    n_coarse_rules=70, target_fine_rules=30000, n_coarse_unaries=12, n_words=300)
+    elif size == "big":
+        # 25-33 refinements per coarse symbol: the flat-tile inside pass cuts
+        # each pair into 16 + 16 + rest sub-tiles and blocks of more than 32
+        # targets into runs of 32
+        c, f = synth.split_grammar(seed=12, n_coarse_nt=5, n_coarse_pt=4, max_split=40, mean_split=30.0,
+                                   n_coarse_rules=60, target_fine_rules=60000, n_coarse_unaries=10, n_words=300)
     elif size == "medium":
         c, f = synth.split_grammar(seed=4, n_coarse_nt=10, n_coarse_pt=8, max_split=8, mean_split=6.0,
                                    n_coarse_rules=120, target_fine_rules=20000, n_coarse_unaries=20, n_words=500)

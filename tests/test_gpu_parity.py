@@ -104,9 +104,9 @@ def test_wide_grammar_split_cells_bit_exact():
 
 
 def test_deep_refinements_bit_exact():
-    """Coarse symbols with up to 30 refinements: the fine kernel's
-    outer products run on all three of its paths (both operands staged by one
-    load, staged separately, and the unstaged loop for larger tiles)."""
+    """Coarse symbols with up to 17 refinements: tiles of every lane-grid
+    shape of the flat-tile outer product, and pairs just over 16 members cut
+    into a 16-member and a 1-member sub-tile."""
     levels = split_levels("viterbi", "deep")
     sents = split_sentences(24, seed=67, n_words=300, mean=16, hi=30)
     P = gpu(levels, "split_deep")
@@ -117,6 +117,32 @@ def test_deep_refinements_bit_exact():
     assert np.array_equal(bits(P.debug_copy(0, "inside")), bits(r.chart(0, "inside")))
     assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
     assert np.array_equal(nodes, r.trees())
+
+
+@pytest.mark.parametrize("lengths", ["short", "long"])
+def test_big_tiles_sub_tiled_bit_exact(lengths):
+    """25-33 refinements per coarse symbol: the fine inside pass runs the
+    flat-tile form on 16 x 16 sub-tiles of each pair (16 + 16 + rest per
+    side), with blocks of more than 32 targets cut into runs.  Short
+    sentences, and 41-100 words (two 64-split liveness chunks)."""
+    levels = split_levels("viterbi", "big")
+    if lengths == "short":
+        sents = split_sentences(32, seed=83, n_words=300, mean=14, hi=30)
+    else:
+        rng = np.random.default_rng(84)
+        sents = [rng.integers(0, 300, size=n).astype(np.int32) for n in (41, 64, 65, 77, 100)]
+    P = gpu(levels, "split_big")
+    words, offsets, _ = pack_sentences(sents)
+    nodes, st = P.parse_ids(words, offsets)
+    assert (st == 0).all()
+    r = oracle.run(levels, sents, mode="parse")
+    assert np.array_equal(bits(P.debug_copy(0, "inside")), bits(r.chart(0, "inside")))
+    m, _, _ = r.masks(0)
+    assert np.array_equal(P.debug_copy(0, "masks"), m)
+    assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
+    assert np.array_equal(nodes, r.trees())
+    # the fine level really runs the flat-tile inside pass
+    assert P.autotune(words, offsets)["levels"][1] == "pair-factored, flat-tile inside"
 
 
 def test_bench_grammar_bit_exact():
