@@ -335,8 +335,9 @@ def run_ours(args):
     words, offsets, lens = pack_sentences(sents)
     P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, device=local, max_length=MAX_LEN,
                  use_graphs=True)
-    # the library's autotuner picks the gather form per level and the split
-    # waves on a sample of the workload, before any timing
+    # the library's autotuner picks the split waves and, per level, the span
+    # band of the flat-tile inside form on a sample of the workload, before
+    # any timing
     tw, to, _ = pack_sentences(sents[:args.tune_sample]) if args.tune_sample > 0 else (None, None, None)
     tuned = P.autotune(tw, to) if args.tune_sample > 0 else None
     for _ in range(args.warmup):
@@ -577,8 +578,11 @@ def run_long(args):
     levels, path, sents = long_workload(args.seed, args.long_sentences)
     words, offsets, _ = pack_sentences(sents)
     rows = []
+    tune = min(len(sents), 200) if args.tune_sample > 0 else 0
+    tw, to, _ = pack_sentences(sents[:tune]) if tune else (None, None, None)
     for thr in (-6.0, -9.0, -12.0):
         P = CLParser(path, max_alloc_size=args.mem_gb << 30, profile=True, max_length=100, prune_threshold=thr)
+        tuned = P.autotune(tw, to) if tune else None
         nodes, st = P.parse_ids(words, offsets)  # warm-up
         assert (st == 0).all()
         t0 = time.perf_counter()
@@ -587,7 +591,7 @@ def run_long(args):
         s = P.stats()
         rows.append({"prune_threshold": thr, "sentences_per_s": round(len(sents) / (s["ms_device"] / 1e3), 2),
                      "e2e_sentences_per_s": round(len(sents) / api, 2), "batches": int(s["batches"]),
-                     "fine_work_units": P.level_work(1)[0],
+                     "fine_work_units": P.level_work(1)[0], "autotuned": tuned,
                      "passes_ms": {f"level{l}": [round(v, 1) for v in P.pass_ms(l)[0]] for l in range(2)}})
         log(f"long, threshold {thr}: {rows[-1]}")
         P.release()

@@ -164,12 +164,26 @@ puck_status puck_parser_pass_ms(const puck_parser* p, int32_t level, double out[
  * keeps, for the whole parser, how many waves of CTAs the cells of a span
  * launch that does not fill the GPU are split to fill (1, 2 or 4).  chosen
  * (levels + 1 entries, may be NULL) receives each level's gather form (0
- * target-major, 2 pair-factored, 3 pair-factored with the flat-tile inside
- * pass; the archive's choice) and the waves x 100.
+ * target-major, 2 pair-factored; the archive's choice) and the waves x 100.
+ * Per level with the flat-tile layout it also chooses the span band whose
+ * inside launches run the flat-tile form (puck_parser_flat_from).
  * Results do not depend on the choice (Viterbi bit-identical; Real sums
  * reorder). */
 puck_status puck_parser_autotune(puck_parser* p, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
                                  int32_t* chosen);
+
+/* First span whose inside launch of `level` runs the flat-tile form: 16 x 16
+ * outer-product tiles (the sub-tiles of a pair-factored level's coarse
+ * pairs, or groups of 16 coarse ids of a target-major Viterbi level) with
+ * four-rule records; shorter spans run the level's own form.  0: no span
+ * (or no flat-tile layout), -1: bad level.  By default every span of a
+ * pair-factored Viterbi level; puck_parser_autotune may choose another band.
+ * Results do not depend on it (max-plus, bit-identical). */
+int32_t puck_parser_flat_from(const puck_parser* p, int32_t level);
+/* Pins that band: span >= 2 runs the flat-tile form from that span on, 0 at
+ * no span.  PUCK_ERR_INVALID_ARG for a bad level, span 1, or span > 0 on a
+ * level without the flat-tile layout. */
+puck_status puck_parser_set_flat_from(puck_parser* p, int32_t level, int32_t span);
 
 /* 1 if `level` runs its inside binary sums on tensor cores (options
  * tensor_cores and a level the form covers), 0 if not (why, may be NULL,

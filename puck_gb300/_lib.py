@@ -53,7 +53,7 @@ class ServerStats(ctypes.Structure):
 EXPORTS = ("puck_default_options", "puck_default_compile_options", "puck_compile_grammar", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
            "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
-           "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_parser_tensor_cores", "puck_mbr_decode_static",
+           "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_parser_flat_from", "puck_parser_set_flat_from", "puck_parser_tensor_cores", "puck_mbr_decode_static",
            "puck_tc_selftest", "puck_server_create",
            "puck_server_destroy", "puck_server_now_ns", "puck_server_submit", "puck_server_poll",
            "puck_server_take", "puck_server_get_stats", "puck_server_pass_ms", "puck_last_error")
@@ -105,6 +105,10 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_parser_autotune.restype = I
         L.puck_parser_tensor_cores.argtypes = [P, I, ctypes.c_char_p, ctypes.c_size_t]
         L.puck_parser_tensor_cores.restype = I
+        L.puck_parser_flat_from.argtypes = [P, I]
+        L.puck_parser_flat_from.restype = I
+        L.puck_parser_set_flat_from.argtypes = [P, I, I]
+        L.puck_parser_set_flat_from.restype = I
         L.puck_tc_selftest.argtypes = [I, I, I, P, P, P]
         L.puck_tc_selftest.restype = I
         L.puck_server_create.restype = P

@@ -91,8 +91,9 @@ __host__ __device__ __forceinline__ int mtile_floats(const DevLevel& L, bool wit
   return with_stage && L.flat_inside ? L.flat_mtile : L.max_mtile;
 }
 
-// with_stage: the per-warp operand stage of the Viterbi inside pass
-__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage) {
+// with_stage: the per-warp operand stage of the Viterbi inside pass;
+// pairs: a pair-factored kernel (MODE 2 or 3)
+__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage, bool pairs) {
   Smem m;
   const int cs = L.cell_size;
   m.P = base;
@@ -103,7 +104,7 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
   m.list = nullptr;
   m.slist = nullptr;
   m.mtile = mtile_floats(L, with_stage);
-  if (L.mode == 2) {
+  if (pairs) {
     if (with_stage) {
       m.stage = rest;
       rest += (blockDim.x >> 5) * kStageFloats;
@@ -231,6 +232,13 @@ __device__ void gather_targets(const DevJob& J, const DevLevel& L, bool gated, f
 }
 
 __device__ __forceinline__ bool bit(const int* words, int c) { return (words[c >> 5] >> (c & 31)) & 1; }
+
+// Whether pair key c has a live member in the liveness words: key = one
+// coarse symbol (grp 1), or the group of 16 coarse ids 16c .. 16c + 15
+// (grp 16, DevLevel::pair_group).
+__device__ __forceinline__ bool key_live(const int* words, int c, int grp) {
+  return grp <= 1 ? bit(words, c) : (((unsigned)words[c >> 1] >> ((c & 1) * 16)) & 0xffffu) != 0u;
+}
 
 template <int S>
 __device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned long long& corner) {
@@ -363,7 +371,7 @@ __device__ __forceinline__ void flat_rules(const DevJob& J, const CellCtx& X, in
 // pairs from a shared counter (this part's pairs are list positions g,
 // g + G, g + 2G, ...), so a warp that drew cheap pairs takes more of them.
 __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, CellCtx& X, int c0, int nc, int nlive,
-                                           float* Mw, float* P, unsigned long long& work,
+                                           int grp, float* Mw, float* P, unsigned long long& work,
                                            unsigned long long& corner) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4* st4 = reinterpret_cast<float4*>(sm.stage + warp * kStageFloats);
@@ -376,9 +384,10 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
     const int p = sm.list[i];
     const int4 D = __ldg(J.pair_desc + p);
     const int ca = D.w & 255, cb = (D.w >> 8) & 255;
-    const unsigned lo = __ballot_sync(kFull, lane < nc && bit(X.la[lane], ca) && bit(X.lb[lane], cb));
-    const unsigned hi =
-        __ballot_sync(kFull, lane + 32 < nc && bit(X.la[lane + 32], ca) && bit(X.lb[lane + 32], cb));
+    const unsigned lo =
+        __ballot_sync(kFull, lane < nc && key_live(X.la[lane], ca, grp) && key_live(X.lb[lane], cb, grp));
+    const unsigned hi = __ballot_sync(
+        kFull, lane + 32 < nc && key_live(X.la[lane + 32], ca, grp) && key_live(X.lb[lane + 32], cb, grp));
     const unsigned long long m = (unsigned long long)lo | ((unsigned long long)hi << 32);
     // the pair's live splits in order, then three repeats of the last one
     const unsigned below = (1u << lane) - 1u;
@@ -408,7 +417,12 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
 template <int S, bool FLAT = false>
 __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
                              CellCtx& X) {
-  const int ms = L.mask_size, nco = L.n_coarse;
+  const int ms = L.mask_size, grp = FLAT ? L.pair_group : 1;
+  const int nkeys = grp <= 1 ? L.n_coarse : (L.n_coarse + 15) >> 4;  // pair keys: coarse symbols or groups
+  // the pair list of this kernel's form (the flat-tile form has its own, of sub-tiles)
+  const int npair = FLAT ? J.fnpair : J.npair;
+  const int* pair_key = FLAT ? J.fpair_key : J.pair_key;
+  const int* pair_gate = FLAT ? J.fpair_gate : J.pair_gate;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int* aoff = J.a_is_t ? L.t_mem_off : L.nt_mem_off;
   const int* amem = J.a_is_t ? L.t_mem : L.nt_mem;
@@ -417,12 +431,12 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
   float* Mw = sm.M + warp * sm.mtile;
   const int nsp = X.nsp;
   unsigned long long work = 0, corner = 0;
-  if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage && threadIdx.x < 4 && nsp > 0) {
+  if (FLAT && threadIdx.x < 4 && nsp > 0) {
     // the split lists run in groups of four: repeat the last split
     X.aptr[nsp + threadIdx.x] = X.aptr[nsp - 1];
     X.bptr[nsp + threadIdx.x] = X.bptr[nsp - 1];
   }
-  if (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage && lane < 16) {
+  if (FLAT && lane < 16) {
     // the -inf rows of the flat-tile stage (rows 16 and kStageRowB + 16 of both buffers)
     const int row = (lane >> 3) * kStageRows + ((lane & 4) ? kStageRowB + 16 : 16);
     sm.stage[warp * kStageFloats + row * 4 + (lane & 3)] = -CUDART_INF_F;
@@ -447,13 +461,13 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
       X.next = 0;
     }
     __syncthreads();
-    // pl[ca] = union over splits with a live ca on the left of the right-hand live sets
-    for (int ca = threadIdx.x; ca < nco; ca += blockDim.x) {
+    // pl[ca] = union over splits with a live key ca on the left of the right-hand live sets
+    for (int ca = threadIdx.x; ca < nkeys; ca += blockDim.x) {
       unsigned acc[kMaxMask];
 #pragma unroll
       for (int w = 0; w < kMaxMask; ++w) acc[w] = 0u;
       for (int s = 0; s < nc; ++s) {
-        if (bit(X.la[s], ca)) {
+        if (key_live(X.la[s], ca, grp)) {
 #pragma unroll
           for (int w = 0; w < kMaxMask; ++w)
             if (w < ms) acc[w] |= (unsigned)X.lb[s][w];
@@ -465,16 +479,16 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
     // compact the live pairs (coarse liveness, then the OR of their segments' bits)
-    for (int base = 0; base < J.npair; base += blockDim.x) {
+    for (int base = 0; base < npair; base += blockDim.x) {
       const int k = base + threadIdx.x;
       bool live = false;
-      if (k < J.npair) {
-        const int key = __ldg(J.pair_key + k);
+      if (k < npair) {
+        const int key = __ldg(pair_key + k);
         const int ca = key & 255, cb = (key >> 8) & 255;
-        live = (sm.pl[ca * ms + (cb >> 5)] >> (cb & 31)) & 1u;
+        live = key_live(reinterpret_cast<const int*>(sm.pl) + ca * ms, cb, grp);
         if (live && gated) {
           bool hit = false;
-          for (int i = 0; i < ms; ++i) hit |= (__ldg(J.pair_gate + k * ms + i) & X.gate[i]) != 0;
+          for (int i = 0; i < ms; ++i) hit |= (__ldg(pair_gate + k * ms + i) & X.gate[i]) != 0;
           live = hit;
         }
       }
@@ -495,12 +509,11 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
     const int nlive = X.nlive;
-    if (FLAT || (S == SEMI_VITERBI && J.interleaved == 3 && sm.stage)) {
-      flat_pairs(J, sm, X, c0, nc, nlive, Mw, P, work, corner);
+    if (FLAT) {
+      flat_pairs(J, sm, X, c0, nc, nlive, grp, Mw, P, work, corner);
       __syncthreads();
       continue;
     }
-    if (FLAT) continue;  // not reached
     for (int i = X.g * nwarps + warp; i < nlive; i += X.G * nwarps) {
       const int p = sm.list[i];
       const int key = __ldg(J.pair_key + p);
@@ -841,7 +854,7 @@ __global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk, S == SEMI_VITERBI);
+  const Smem sm = carve(smem, L, chunk, S == SEMI_VITERBI, MODE >= 2);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -907,6 +920,12 @@ __global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
+      // Every warp leaves this job before the next job's split list, pair
+      // list and gates are written: a job without allowed splits returns
+      // from the gather without a barrier, and a warp still reading its
+      // split count would otherwise run this job's tables over the next
+      // job's splits and pair list.
+      __syncthreads();
     }
   }
   __syncthreads();
@@ -942,7 +961,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk, false);
+  const Smem sm = carve(smem, L, chunk, false, MODE >= 2);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -1017,6 +1036,9 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
     for (int job = 0; job < 4; ++job) {
       const int jid = job == 0 ? OUT_R_TN : job == 1 ? OUT_L_NT : job == 2 ? OUT_L_NN : OUT_R_NN;
       if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
+      // no split at the sentence's edges: a right-child job needs a parent
+      // starting before b, a left-child job one ending after e
+      if ((jid == OUT_R_TN || jid == OUT_R_NN) ? b < 1 : e + 1 > n) continue;
       if (jid == OUT_L_NN) {
         range_splits(e + 1, n + 1, true, [&](int sp, long long& c1, long long& c2) {
           c1 = BOT(b, sp);
@@ -1037,6 +1059,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
+      __syncthreads();
     }
   }
   __syncthreads();
@@ -1061,6 +1084,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
     for (int job = 0; job < 4; ++job) {
       const int jid = job == 0 ? OUT_L_TT : job == 1 ? OUT_R_NT : job == 2 ? OUT_L_TN : OUT_R_TT;
       if (L.jobs[jid].n_tgt == 0 || L.jobs[jid].nseg == 0) continue;
+      if ((jid == OUT_R_NT || jid == OUT_R_TT) ? b < 1 : b + 2 > n) continue;  // as above
       if (jid == OUT_R_NT) {
         range_splits(0, b, false, [&](int sp, long long& c1, long long& c2) {
           c1 = TOP(sp, b);
@@ -1081,6 +1105,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, Q, sm, chunk, X);
+      __syncthreads();
     }
   }
   __syncthreads();
@@ -1156,9 +1181,9 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
-size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage) {
+size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs) {
   const size_t cs = L.cell_size;
-  if (L.mode == 2)
+  if (pairs)
     return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + mtile_floats(L, with_stage))) *
                sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int) +
@@ -1198,7 +1223,7 @@ cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, 
                         int max_span, const float* inside_c, float* inside, float* outside, DevLive V, Counters C,
                         cudaStream_t st) {
   const int chunk = pick_split_chunk(L.cell_size, max_span);
-  const size_t smem = pass_smem_bytes(L, chunk, inside_pass && S == SEMI_VITERBI);
+  const size_t smem = pass_smem_bytes(L, chunk, inside_pass && S == SEMI_VITERBI, MODE >= 2);
   const unsigned grid = (unsigned)W.nunits;
   if (inside_pass) {
     if (cudaError_t e = set_smem(k_inside_span<S, MODE>, smem); e != cudaSuccess) return e;
@@ -1217,7 +1242,9 @@ cudaError_t launch_any(bool inside_pass, const DevLevel& L, const DevBatch& B, c
   const bool pairs = L.mode == 2;
   switch (L.semiring) {
     case SEMI_VITERBI:
-      if (pairs && inside_pass && L.flat_inside)
+      // the flat-tile inside pass (its pairs: of coarse symbols, or of
+      // groups of coarse ids on a target-major level)
+      if (inside_pass && L.flat_inside)
         return launch_pass<SEMI_VITERBI, 3>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
       return pairs ? launch_pass<SEMI_VITERBI, 2>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st)
                    : launch_pass<SEMI_VITERBI, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);

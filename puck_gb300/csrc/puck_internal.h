@@ -38,7 +38,7 @@ struct DevJob {
   int a_is_t, b_is_t;
   int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs):
                           // 1 mixed-target slices, 2 one target per lane slice (slice length a
-                          // multiple of 4), 3 the flat-tile layout below
+                          // multiple of 4)
   const int* pair_key;    // [npair] ca | cb << 8
   const int* pair_gate;   // [npair * mask_size] OR of the pair's segment bits
   const int* pair_blk;    // [npair + 1] block range
@@ -46,16 +46,23 @@ struct DevJob {
   const int* blk_ptr;     // [nblk + 1] rule range, each a multiple of 32 (lane-interleaved, padded)
   const int* blk_nrule;   // [nblk] rules of the block before padding
   const int2* pair_rules;   // {(j * nz + k) | target << 16, bits(w)}
-  // Flat-tile layout (interleaved == 3; Viterbi inside jobs whose every pair
-  // has contiguous operand members, at most 16 per side, and whose blocks
-  // have at most 32 targets).  A pair's outer product M[e], e = j * nz + k,
-  // is held one entry per lane and slot (e = lane + 32 * slot).  A block's
-  // rules keep one target per lane slice; each lane's slice is stored as
-  // records of four rules: their tile entries e (one byte each) and their
-  // weights (padding: weight -inf).  The rules of a record position are
-  // ordered so that the 32 lanes' entries fall in distinct shared-memory
-  // banks where the slices allow.
-  const int4* pair_desc;  // [npair] {first A member | first B member << 16, first block,
+  // Flat-tile layout (flat != 0; Viterbi inside jobs whose pairs have
+  // contiguous operand members; run by the MODE 3 kernels).  Pairs with more
+  // than 16 members on a side are cut into sub-tiles of at most 16 x 16, each
+  // a pair of this layout's own list (fnpair, fpair_key, fpair_gate); on a
+  // level with pair_group 16 the keys are groups of 16 coarse ids.  A
+  // sub-tile's outer product M[e], e = j * nz + k, is held one entry per lane
+  // and slot (e = lane + 32 * slot).  A block's rules (at most 32 targets)
+  // keep one target per lane slice; each lane's slice is stored as records of
+  // four rules: their tile entries e (one byte each) and their weights
+  // (padding: weight -inf).  The rules of a record position are ordered so
+  // that the 32 lanes' entries fall in distinct shared-memory banks where the
+  // slices allow.
+  int flat;
+  int fnpair;
+  const int* fpair_key;   // [fnpair] pair key ca | cb << 8 of each sub-tile
+  const int* fpair_gate;  // [fnpair * mask_size] OR of the sub-tile's segment bits
+  const int4* pair_desc;  // [fnpair] {first A member | first B member << 16, first block,
                           //          ny | nz << 8 | blocks << 16, ca | cb << 8}
   const int4* fr_blk;     // [nblk] {segment, first record, end record, rules}; records of a
                           // block: 32 lanes x steps
@@ -77,9 +84,14 @@ struct DevLevel {
   int max_npair;    // largest pair count of any job (shared-memory list size)
   int max_mtile;    // largest ny * nz of any pair (per-warp outer-product tile)
   int tc_binary;    // sum-product inside pass: binary sums already in the bot cells (tensor-core form)
-  int flat_inside;  // every inside job with rules is in the flat-tile form (DevJob::interleaved == 3)
+  int flat_inside;  // every inside job with rules has the flat-tile layout (DevJob::flat); the
+                    // host clears it in its copy of a level for launches of the other form
   int flat_mtile;   // largest ny * nz of any flat-tile sub-tile (<= 256); the M tile of the
                     // Viterbi inside kernel when flat_inside
+  int pair_group;   // coarse ids per pair key of the flat-tile tables: 1 (pairs of coarse
+                    // symbols) or 16 (a target-major level whose coarse ids each have at
+                    // most one member per role: pairs of groups of 16 coarse ids, liveness
+                    // tested on 16-bit halves of the liveness words)
   const int* nt_mem_off;  // [n_coarse + 1] coarse -> nonterminal members
   const int* nt_mem;
   const int* t_mem_off;   // [n_coarse + 1] coarse -> terminal members
@@ -212,7 +224,7 @@ cudaError_t launch_mbr_decode(const DevBatch& B, const DevWork& W, const DevMask
 cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
                                const float* inside, const double* part_scale, float* log_z, cudaStream_t st);
 
-size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage);
+size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs);
 
 // Tensor-core inside pass: the binary sums of the cells of one span.  cells
 // holds (sentence, begin) pairs; 128 cells per tile, one CTA per tile and

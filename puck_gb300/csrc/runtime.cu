@@ -305,19 +305,15 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
 // targets.  Each target of a block gets lanes in proportion to its rule
 // count (at least one); a lane's slice is stored as records of four rules,
 // padded with weight -inf (the max-plus zero, which never changes a cell).
-// The job's pair list (npair, pair_key, pair_gate) becomes the sub-tile
-// list.  *mtile receives the largest sub-tile.  Returns false, uploading
+// The sub-tiles form the layout's own pair list (fnpair, fpair_key,
+// fpair_gate).  *mtile receives the largest sub-tile.  Returns false, uploading
 // nothing, when the job does not qualify.
-bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int ntgt, int64_t npk,
-                      const int* pk, const int* pbk, const int* bs, const int* bp, const int* pr, const float* pw,
-                      const int* seg_bits, int nseg, int ms, int* mtile) {
-  static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
-  static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
+// ao/am and bo/bm: CSR from pair key to the operands' members (in the
+// operand roles' index spaces) for the left and right operands.
+bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const int* pk, const int* pbk,
+                      const int* bs, const int* bp, const int* pr, const float* pw, const int* seg_bits, int nseg,
+                      int ms, const int* ao, const int* am, const int* bo, const int* bm, int* mtile) {
   constexpr int kSub = 16;  // largest sub-tile side
-  const int* ao = L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
-  const int* am = L.get<int>(a_t[j] ? "t_mem" : "nt_mem", "i4", nullptr);
-  const int* bo = L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr);
-  const int* bm = L.get<int>(b_t[j] ? "t_mem" : "nt_mem", "i4", nullptr);
   auto contiguous = [](const int* off, const int* mem, int c) {
     for (int i = off[c]; i < off[c + 1]; ++i)
       if (mem[i] != mem[off[c]] + (i - off[c])) return false;
@@ -478,7 +474,7 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, i
       }
   }
   if (desc.size() > (size_t)INT32_MAX / 32) return false;
-  J.npair = (int)desc.size();
+  J.fnpair = (int)desc.size();
   if (desc.empty()) desc.push_back(make_int4(0, 0, 0, 0));  // a job without rules still gets (never read) tables
   if (key.empty()) key.push_back(0);
   if (gate.empty()) gate.assign(std::max(ms, 1), 0);
@@ -488,8 +484,9 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, i
     idx.push_back(0u);
     w.push_back(make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
   }
-  J.pair_key = static_cast<const int*>(D.upload(key.data(), key.size() * sizeof(int)));
-  J.pair_gate = static_cast<const int*>(D.upload(gate.data(), gate.size() * sizeof(int)));
+  J.fpair_key = static_cast<const int*>(D.upload(key.data(), key.size() * sizeof(int)));
+  J.fpair_gate = static_cast<const int*>(D.upload(gate.data(), gate.size() * sizeof(int)));
+  J.flat = 1;
   J.pair_desc = static_cast<const int4*>(D.upload(desc.data(), desc.size() * sizeof(int4)));
   J.fr_blk = static_cast<const int4*>(D.upload(blk.data(), blk.size() * sizeof(int4)));
   J.fr_tgt = static_cast<const int*>(D.upload(tgt.data(), tgt.size() * sizeof(int)));
@@ -497,6 +494,89 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, i
   J.fr_w = static_cast<const float4*>(D.upload(w.data(), w.size() * sizeof(float4)));
   *mtile = std::max(*mtile, max_tile);
   return true;
+}
+
+// Flat-tile tables over groups of coarse ids for a target-major Viterbi
+// level whose coarse map rises strictly along each role's symbols (the top
+// level of a cascade: one symbol per coarse id).  Group g holds the symbols
+// of coarse ids 16g .. 16g + 15, a contiguous run of at most 16 symbols per
+// role, so every pair of groups is one flat tile.  Rules come from the
+// job's target-major table, grouped by (group of a, group of b), then by
+// segment and target.  Returns false, uploading nothing, when the level's
+// coarse maps do not rise strictly.
+bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int* mtile) {
+  static const bool a_t[4] = {false, false, true, true};
+  static const bool b_t[4] = {false, true, false, true};
+  const std::string n = kJobNames[j];
+  const int* ntc = L.get<int>("nt_coarse", "i4", nullptr);
+  const int* tc = L.get<int>("t_coarse", "i4", nullptr);
+  // CSR from group to its members, per role
+  auto groups = [&](const int* coarse, int nsym, std::vector<int>& off, std::vector<int>& mem) {
+    const int ng = (L.n_coarse + 15) / 16;
+    off.assign(ng + 1, 0);
+    mem.clear();
+    for (int i = 0; i < nsym; ++i) {
+      if (i > 0 && coarse[i] <= coarse[i - 1]) return false;
+      ++off[coarse[i] / 16 + 1];
+      mem.push_back(i);
+    }
+    for (int g = 0; g < ng; ++g) off[g + 1] += off[g];
+    return true;
+  };
+  std::vector<int> nt_off, nt_mem, t_off, t_mem;
+  if (!groups(ntc, L.n_nt, nt_off, nt_mem) || !groups(tc, L.n_t, t_off, t_mem)) return false;
+  const std::vector<int>& ao = a_t[j] ? t_off : nt_off;
+  const std::vector<int>& am = a_t[j] ? t_mem : nt_mem;
+  const std::vector<int>& bo = b_t[j] ? t_off : nt_off;
+  const std::vector<int>& bm = b_t[j] ? t_mem : nt_mem;
+  const int* ca_of = a_t[j] ? tc : ntc;
+  const int* cb_of = b_t[j] ? tc : ntc;
+  int64_t nrow = 0, nab = 0;
+  const int* rowptr = L.get<int>(n + "/rowptr", "i4", &nrow);
+  const int* ab = L.get<int>(n + "/ab", "i4", &nab);
+  const float* w = L.get<float>(n + "/w", "f4", nullptr);
+  const int* tseg = L.get<int>(n + "/tgt_seg", "i4", nullptr);
+  const int ntgt = (int)(nrow - 1);
+  struct R {
+    int key, seg, t, jk;
+    float w;
+  };
+  std::vector<R> rs;
+  rs.reserve(nab);
+  for (int t = 0; t < ntgt; ++t)
+    for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) {
+      const int a = ab[r] & 0xffff, b = (int)((unsigned)ab[r] >> 16);
+      const int ga = ca_of[a] / 16, gb = cb_of[b] / 16;
+      const int ja = a - am[ao[ga]], kb = b - bm[bo[gb]];
+      if (tseg[t] < 0 || ja < 0 || ja >= ao[ga + 1] - ao[ga] || kb < 0 || kb >= bo[gb + 1] - bo[gb]) return false;
+      rs.push_back({ga | gb << 8, tseg[t], t, ja | kb << 8, w[r]});
+    }
+  std::sort(rs.begin(), rs.end(), [](const R& x, const R& y) {
+    if (x.key != y.key) return x.key < y.key;
+    if (x.seg != y.seg) return x.seg < y.seg;
+    if (x.t != y.t) return x.t < y.t;
+    return x.jk < y.jk;
+  });
+  std::vector<int> pk, pbk, bs, bp, pr;
+  std::vector<float> pw;
+  for (size_t r = 0; r < rs.size(); ++r) {
+    const bool new_pair = r == 0 || rs[r].key != rs[r - 1].key;
+    if (new_pair) {
+      pk.push_back(rs[r].key);
+      pbk.push_back((int)bs.size());
+    }
+    if (new_pair || rs[r].seg != rs[r - 1].seg) {
+      bs.push_back(rs[r].seg);
+      bp.push_back((int)r);
+    }
+    pr.push_back(rs[r].jk | rs[r].t << 16);
+    pw.push_back(rs[r].w);
+  }
+  pbk.push_back((int)bs.size());
+  bp.push_back((int)rs.size());
+  return build_flat_tiles(D, J, ntgt, (int64_t)pk.size(), pk.data(), pbk.data(), bs.data(), bp.data(), pr.data(),
+                          pw.data(), L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size, ao.data(),
+                          am.data(), bo.data(), bm.data(), mtile);
 }
 
 }  // namespace
@@ -682,12 +762,15 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
     J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
-    // Viterbi inside jobs take the flat-tile form where it applies (it
-    // replaces the pair list by its sub-tile list)
-    if (interleave && build_flat_tiles(D, J, L, j, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr),
-                                       bp, pr, pw, L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size,
-                                       &d.flat_mtile))
-      J.interleaved = 3;
+    // Viterbi inside jobs also get the flat-tile layout where it applies
+    if (interleave &&
+        build_flat_tiles(D, J, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw,
+                         L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size,
+                         L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
+                         L.get<int>(a_t[j] ? "t_mem" : "nt_mem", "i4", nullptr),
+                         L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
+                         L.get<int>(b_t[j] ? "t_mem" : "nt_mem", "i4", nullptr), &d.flat_mtile))
+      d.max_npair = std::max(d.max_npair, J.fnpair);
     J.pair_blk = up<int>(D, L, n + "/pair_blk", "i4");
     J.blk_seg = up<int>(D, L, n + "/blk_seg", "i4");
     J.blk_ptr = static_cast<const int*>(D.upload(dev_bp.data(), dev_bp.size() * sizeof(int)));
@@ -704,10 +787,32 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
   }
   d.flat_inside = 1;
   for (int j = puck::IN_NN; j <= puck::IN_TT; ++j)
-    if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0 && d.jobs[j].interleaved != 3) d.flat_inside = 0;
+    if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0 && !d.jobs[j].flat) d.flat_inside = 0;
+  d.pair_group = 1;
   {
     const int* nn_mode = L.get<int>("in_NN/pair_mode", "i4", nullptr);
     d.mode = (nn_mode[0] == 2 && L.semiring != puck::SEMI_LOGSUM) ? 2 : 0;
+    // A target-major Viterbi level (the coarse level of a cascade, one
+    // symbol per coarse id) gets its flat-tile layout over groups of 16
+    // coarse ids, which replace its one-symbol pairs.
+    if (d.mode == 0 && L.semiring == puck::SEMI_VITERBI) {
+      int mt = 0;
+      bool ok = true;
+      for (int j = puck::IN_NN; ok && j <= puck::IN_TT; ++j)
+        if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0) ok = build_group_tiles(D, d.jobs[j], L, j, &mt);
+      if (ok) {
+        d.pair_group = 16;
+        d.flat_mtile = mt;
+        d.flat_inside = 1;
+        for (int j = puck::IN_NN; j <= puck::IN_TT; ++j) d.max_npair = std::max(d.max_npair, d.jobs[j].fnpair);
+      } else {
+        d.flat_inside = 0;  // group tables in some jobs, one-symbol pairs in others: not used
+      }
+    }
+    // The flat-tile inside pass is ready; by default it runs on the
+    // pair-factored levels (the parser's autotuner chooses per span band).
+    D.flat_ready = d.flat_inside != 0;
+    d.flat_inside = D.flat_ready && d.mode == 2;
     d.nt_mem_off = up<int>(D, L, "nt_mem_off", "i4");
     d.nt_mem = up<int>(D, L, "nt_mem", "i4");
     d.t_mem_off = up<int>(D, L, "t_mem_off", "i4");
@@ -958,6 +1063,8 @@ struct LevelBufs {
 
 }  // namespace
 
+constexpr int kNoFlat = 1 << 30;  // flat_from of a level that never runs the flat-tile form
+
 struct puck_parser {
   const puck_grammar* g = nullptr;
   puck_options opt{};
@@ -982,9 +1089,11 @@ struct puck_parser {
   std::vector<std::array<cudaGraphExec_t, 2>> graphs;
   int64_t graph_updates = 0, graph_instantiations = 0;
   // autotuned policy: per level the gather form (-1: the archive's choice,
-  // 0 target-major, 2 pair-factored), and the waves of CTAs that long cells
-  // are split to fill
+  // 0 target-major, 2 pair-factored), the first span whose inside launch
+  // runs the flat-tile form (kNoFlat: none), and the waves of CTAs that long
+  // cells are split to fill
   std::vector<int> tuned_mode;
+  std::vector<int> flat_from;
   double waves = 2.0;
 };
 
@@ -1228,7 +1337,10 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
           W1.ways_all = 1;
           CUDA_TRY(puck::launch_inside_span(D, B, W1, MM, max_len, inside, V, C, st));
         } else {
-          CUDA_TRY(puck::launch_inside_span(D, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
+          // the flat-tile form from the level's chosen span on
+          puck::DevLevel Ds = D;
+          Ds.flat_inside = P->levels[l]->flat_ready && span >= P->flat_from[l];
+          CUDA_TRY(puck::launch_inside_span(Ds, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
         }
         ++LC[0];
       }
@@ -1521,10 +1633,14 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
     P->level_work.assign(nl, std::array<int64_t, 2>{0, 0});
     P->graphs.assign(nl, std::array<cudaGraphExec_t, 2>{nullptr, nullptr});
     P->tuned_mode.assign(nl, -1);
+    P->flat_from.assign(nl, kNoFlat);
     for (int l = 0; l < nl; ++l) {
       P->levels.emplace_back(new LevelDev());
       LevelDev& LD = *P->levels.back();
       build_level(LD, g->levels[l], l < nl - 1 && nl != 1);
+      // by default the flat-tile inside pass runs at every span of the
+      // pair-factored levels that have it
+      if (LD.d.flat_inside) P->flat_from[l] = 2;
       if (P->opt.tensor_cores) {
         if (l == nl - 1) LD.tc_ok = build_tc(LD, g->levels[l], &LD.tc_why);
         else LD.tc_why = "a coarse level of the cascade (it only makes masks)";
@@ -1663,12 +1779,42 @@ puck_status puck_parser_autotune(puck_parser* P, const int32_t* word_ids, const 
     if (best < 0 || t < best) { best = t; best_w = w; }
   }
   P->waves = best_w;
+  // per level with the flat-tile layout, the span band that runs it (the
+  // 16 x 16 tiles: the sub-tiles of the level's pairs, or groups of 16
+  // coarse ids) and the band that keeps the level's own form (the whole
+  // pairs' tiles, or one rule at a time): from span 2, 8, 16 or never
+  for (int l = 0; l < nl; ++l) {
+    if (!P->levels[l]->flat_ready) continue;
+    double best_t = -1.0;
+    int best_f = P->flat_from[l];
+    for (int f : {2, 8, 16, kNoFlat}) {
+      P->flat_from[l] = f;
+      const double t = run(-1);
+      if (t < 0) return PUCK_ERR_CUDA;
+      if (best_t < 0 || t < best_t) { best_t = t; best_f = f; }
+    }
+    P->flat_from[l] = best_f;
+  }
   if (chosen) {
-    for (int l = 0; l < nl; ++l)
-      chosen[l] = P->tuned_mode[l] == 2 && P->levels[l]->d.flat_inside ? 3 : P->tuned_mode[l];
+    for (int l = 0; l < nl; ++l) chosen[l] = P->tuned_mode[l];
     chosen[nl] = (int32_t)(best_w * 100);
   }
   return PUCK_OK;
+}
+
+puck_status puck_parser_set_flat_from(puck_parser* p, int32_t level, int32_t span) {
+  if (!p || level < 0 || level >= (int)p->levels.size() || span < 0 || span == 1 ||
+      (span > 0 && !p->levels[level]->flat_ready)) {
+    set_error("puck_parser_set_flat_from: bad level or span, or a level without the flat-tile layout");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  p->flat_from[level] = span == 0 ? kNoFlat : span;
+  return PUCK_OK;
+}
+
+int32_t puck_parser_flat_from(const puck_parser* p, int32_t level) {
+  if (!p || level < 0 || level >= (int)p->levels.size()) return -1;
+  return p->levels[level]->flat_ready && p->flat_from[level] < kNoFlat ? p->flat_from[level] : 0;
 }
 
 int32_t puck_parser_tensor_cores(const puck_parser* p, int32_t level, char* why, size_t len) {

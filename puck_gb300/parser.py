@@ -319,12 +319,27 @@ class CLParser:
 
     def autotune(self, words: np.ndarray, offsets: np.ndarray) -> dict:
         """Runs the library's autotuner on a sample (word ids + offsets) and
-        returns the chosen gather form per level and the split waves."""
+        returns the gather form per level, the span band of the flat-tile
+        inside form per level and the split waves."""
         nl = len(self.data)
         out = np.zeros(nl + 1, np.int32)
         _lib.check(self._L.puck_parser_autotune(self._p, _ptr(words), _ptr(offsets), len(offsets) - 1, _ptr(out)))
-        names = {0: "target-major", 2: "pair-factored", 3: "pair-factored, flat-tile inside"}
-        return {"levels": [names.get(int(m), str(int(m))) for m in out[:nl]], "waves": int(out[nl]) / 100.0}
+        names = {0: "target-major", 2: "pair-factored"}
+        return {"levels": [names.get(int(m), str(int(m))) for m in out[:nl]],
+                "flat_from": [self.flat_from(l) for l in range(nl)], "waves": int(out[nl]) / 100.0}
+
+    def set_flat_from(self, level: int, span: int) -> None:
+        """Pins the first span whose inside launch of `level` runs the
+        flat-tile form (0: none)."""
+        _lib.check(self._L.puck_parser_set_flat_from(self._p, level, span))
+
+    def flat_from(self, level: int) -> int:
+        """First span whose inside launch of `level` runs the flat-tile form
+        (0: none)."""
+        r = self._L.puck_parser_flat_from(self._p, level)
+        if r < 0:
+            raise ValueError(f"bad level {level}")
+        return r
 
     def tensor_cores(self, level: int):
         """(True, "") if the level's inside binary sums run on tensor cores,

@@ -141,8 +141,8 @@ def test_big_tiles_sub_tiled_bit_exact(lengths):
     assert np.array_equal(P.debug_copy(0, "masks"), m)
     assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
     assert np.array_equal(nodes, r.trees())
-    # the fine level really runs the flat-tile inside pass
-    assert P.autotune(words, offsets)["levels"][1] == "pair-factored, flat-tile inside"
+    # the fine level really runs the flat-tile inside pass, from span 2
+    assert P.flat_from(1) == 2
 
 
 def test_bench_grammar_bit_exact():
@@ -212,6 +212,28 @@ def test_graph_capture_gives_identical_results():
     assert np.array_equal(n2, r2)
 
 
+@pytest.mark.parametrize("size", ["medium", "big"])
+def test_flat_tile_span_bands_bit_exact(size):
+    """Every span band of the flat-tile inside form, on both levels: the
+    coarse level's groups of 16 coarse ids (target-major otherwise) and the
+    fine level's 16 x 16 sub-tiles (the pair form otherwise), switched at
+    span 2, 9, 17 or never.  Charts and trees stay bit-identical."""
+    levels = split_levels("viterbi", size)
+    sents = split_sentences(40, seed=47, n_words=300 if size == "big" else 500, mean=16, hi=30)
+    words, offsets, _ = pack_sentences(sents)
+    r = oracle.run(levels, sents, mode="parse")
+    P = gpu(levels, f"split_{size}")
+    for f0, f1 in ((0, 0), (2, 2), (9, 17), (17, 9), (2, 0), (0, 2)):
+        P.set_flat_from(0, f0)
+        P.set_flat_from(1, f1)
+        assert (P.flat_from(0), P.flat_from(1)) == (f0, f1)
+        nodes, st = P.parse_ids(words, offsets)
+        assert (st == 0).all()
+        assert np.array_equal(bits(P.debug_copy(0, "inside")), bits(r.chart(0, "inside")))
+        assert np.array_equal(bits(P.debug_copy(1, "inside")), bits(r.chart(1, "inside")))
+        assert np.array_equal(nodes, r.trees())
+
+
 def test_autotune_keeps_results():
     """The autotuner may switch a level's gather form and the split waves;
     Viterbi results stay bit-identical."""
@@ -222,6 +244,7 @@ def test_autotune_keeps_results():
     ref, _ = P.parse_ids(words, offsets)
     choice = P.autotune(words, offsets)
     assert len(choice["levels"]) == 2 and choice["waves"] in (1.0, 2.0, 4.0)
+    assert all(f in (0, 2, 8, 16) for f in choice["flat_from"])
     nodes, st = P.parse_ids(words, offsets)
     assert (st == 0).all() and np.array_equal(nodes, ref)
     r = oracle.run(levels, sents, mode="parse")
