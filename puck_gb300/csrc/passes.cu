@@ -92,7 +92,9 @@ __host__ __device__ __forceinline__ int mtile_floats(const DevLevel& L, bool wit
 }
 
 // with_stage: the per-warp operand stage of the Viterbi inside pass;
-// pairs: a pair-factored kernel (MODE 2 or 3)
+// pairs: a pair-factored kernel (MODE 2 or 3; the outside kernel tests the
+// level's mode at run time instead, which keeps its target-major register
+// allocation free of spills)
 __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage, bool pairs) {
   Smem m;
   const int cs = L.cell_size;
@@ -225,6 +227,7 @@ __device__ void gather_targets(const DevJob& J, const DevLevel& L, bool gated, f
     }
     __syncthreads();
   }
+  if (nsp == 0) __syncthreads();  // see gather()
   if (lane == 0 && (work | corner)) {
     atomicAdd(&X.work, work);
     atomicAdd(&X.corner, corner);
@@ -733,6 +736,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     }
     __syncthreads();
   }
+  if (nsp == 0) __syncthreads();  // see gather()
   if (lane == 0 && (work | corner)) {
     atomicAdd(&X.work, work);
     atomicAdd(&X.corner, corner);
@@ -741,6 +745,17 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
 
 // MODE 0 target-major, 2 pair-factored, 3 pair-factored with every job in
 // the flat-tile form (Viterbi inside passes).
+//
+// The span kernels run their jobs one after another in one CTA, and one warp
+// (or one thread) writes each job's split count, operand pointers, gates and
+// pair list into the CTA's shared bookkeeping.  Every warp must leave a job
+// before the next job's setup is written, or a warp still reading this job's
+// split count would run its tables over the next job's splits and pair list.
+// A gather with splits ends on a barrier that every warp reaches after its
+// last read of them (the last barrier of its chunk loop); one without splits
+// ends on a barrier of its own.  Each warp's copy of the split count is this
+// job's: the next one is written only after all warps passed one of those
+// barriers.
 template <int S, int MODE>
 __device__ __forceinline__ void gather(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
                                        int chunk, CellCtx& X) {
@@ -920,12 +935,6 @@ __global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
-      // Every warp leaves this job before the next job's split list, pair
-      // list and gates are written: a job without allowed splits returns
-      // from the gather without a barrier, and a warp still reading its
-      // split count would otherwise run this job's tables over the next
-      // job's splits and pair list.
-      __syncthreads();
     }
   }
   __syncthreads();
@@ -961,7 +970,7 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk, false, MODE >= 2);
+  const Smem sm = carve(smem, L, chunk, false, MODE == 3 || L.mode == 2);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -1059,7 +1068,6 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, P, sm, chunk, X);
-      __syncthreads();
     }
   }
   __syncthreads();
@@ -1105,7 +1113,6 @@ __global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4
       }
       __syncthreads();
       gather<S, MODE>(L.jobs[jid], L, gated, Q, sm, chunk, X);
-      __syncthreads();
     }
   }
   __syncthreads();
@@ -1228,7 +1235,7 @@ cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, 
   if (inside_pass) {
     if (cudaError_t e = set_smem(k_inside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_inside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside, V, C, chunk);
-  } else if (MODE != 3) {
+  } else if constexpr (MODE != 3) {  // the flat-tile form has no outside pass
     if (cudaError_t e = set_smem(k_outside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_outside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside_c, outside, V, C, chunk);
   }
