@@ -225,7 +225,7 @@ def serving(path, levels, args, device: int):
     sents = synth.lognormal_sentences(args.seed + 1000, n, 23, 1, 60, len(levels[1].lex_offsets) - 1)
     words, offsets, lens = pack_sentences(sents)
     S = CLServer(path, max_alloc_size=args.serve_mem_gb << 30, device=device, max_length=60, collect=False,
-                 profile=True)
+                 profile=True, lanes=args.serve_lanes)
 
     def drain(count, want):
         lat, done_at = [], []
@@ -293,8 +293,9 @@ def serving(path, levels, args, device: int):
                      "pass_ms": {f"level{l}": [round(a - b, 1) for a, b in zip(S.pass_ms(l), pm0[l])]
                                  for l in range(len(levels))}})
         log(f"serving {rate}/s: {rows[-1]}")
+    lanes = S.lanes()
     S.close()
-    return {"sentences_per_rate": n, "lengths": "lognormal mean 23 clipped 1-60",
+    return {"sentences_per_rate": n, "lanes": lanes, "lengths": "lognormal mean 23 clipped 1-60",
             "arrivals": "open-loop Poisson, latency from scheduled arrival to result available on the host",
             "rates": rows}
 
@@ -663,6 +664,7 @@ def main():
     ap.add_argument("--serve-rates", type=lambda v: [float(x) for x in v.split(",") if x], default="1000,2000,3000")
     ap.add_argument("--serve-sentences", type=int, default=6000)
     ap.add_argument("--serve-mem-gb", type=int, default=32)
+    ap.add_argument("--serve-lanes", type=int, default=0, help="server request loops (0: the library's default)")
     ap.add_argument("--tensor-cores", action="store_true",
                     help="mbr config: the fine level's inside binary sums on tcgen05 tensor cores (BF16)")
     ap.add_argument("--config", default="viterbi", choices=["viterbi", "mbr", "long", "small"],

@@ -62,6 +62,9 @@ typedef struct puck_options {
                                  sum-product fine level's inside binary sums run on tcgen05 tensor
                                  cores in BF16 with FP32 accumulation (levels whose structure the
                                  form does not cover, and the server, keep the FP32 path) */
+  int32_t server_lanes;       /* puck_server_create: independent request loops ("lanes"), each with
+                                 its own streams and a share of the memory and slots (0: 2; fewer
+                                 when a share could not hold a few sentences of max_length) */
 } puck_options;
 
 /* One node of a preorder tree (the reference's tree_t, CLViterbi.scala:378):
@@ -244,9 +247,15 @@ puck_status puck_tc_selftest(int32_t device, int32_t k, int32_t n, const uint16_
  * Options as for puck_parser_create: mem_bytes sizes the chart
  * arena, max_batch_sentences caps the resident sentences (0: 65,536),
  * max_length, decode and prune_threshold as for a parse.  submit, poll, take
- * and stats may be called from any thread.  A result does not depend on which
- * other sentences were resident; a one-word sentence parses as in a batch
- * that also holds longer sentences. */
+ * and stats may be called from any thread.  The server runs several lanes
+ * (opts.server_lanes): independent request loops on their own streams over
+ * one copy of the device grammar tables, each with a share of the memory and
+ * slots; a request goes to the lane with the fewest cells in hand, so one
+ * lane's slow cells overlap the other lanes' ticks.  Stats sum over the lanes
+ * (resident_peak and arena_cells_peak: the sum of the lanes' peaks; ms_device:
+ * of their ticks, which overlap).  A result does not depend on which other
+ * sentences were resident or on its lane; a one-word sentence parses as in a
+ * batch that also holds longer sentences. */
 typedef struct puck_server puck_server;
 
 typedef struct puck_server_stats {
@@ -283,6 +292,8 @@ puck_status puck_server_get_stats(const puck_server* s, puck_server_stats* out);
  * With a cascade the coarse levels run as per-admission batches; their whole
  * time is reported as level 0's inside entry. */
 puck_status puck_server_pass_ms(const puck_server* s, int32_t level, double out[5]);
+/* Lanes the server runs (see puck_options.server_lanes). */
+int32_t puck_server_lanes(const puck_server* s);
 
 /* Last error message of the calling thread; returns the full length. */
 size_t puck_last_error(char* buf, size_t len);

@@ -26,7 +26,7 @@ class Options(ctypes.Structure):
     _fields_ = [("mem_bytes", ctypes.c_int64), ("device", ctypes.c_int32), ("profile", ctypes.c_int32),
                 ("decode", ctypes.c_int32), ("max_length", ctypes.c_int32),
                 ("max_batch_sentences", ctypes.c_int32), ("prune_threshold", ctypes.c_float),
-                ("use_graphs", ctypes.c_int32), ("tensor_cores", ctypes.c_int32)]
+                ("use_graphs", ctypes.c_int32), ("tensor_cores", ctypes.c_int32), ("server_lanes", ctypes.c_int32)]
 
 
 class TreeNode(ctypes.Structure):
@@ -56,7 +56,7 @@ EXPORTS = ("puck_default_options", "puck_default_compile_options", "puck_compile
            "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_parser_flat_from", "puck_parser_set_flat_from", "puck_parser_tensor_cores", "puck_mbr_decode_static",
            "puck_tc_selftest", "puck_server_create",
            "puck_server_destroy", "puck_server_now_ns", "puck_server_submit", "puck_server_poll",
-           "puck_server_take", "puck_server_get_stats", "puck_server_pass_ms", "puck_last_error")
+           "puck_server_take", "puck_server_get_stats", "puck_server_pass_ms", "puck_server_lanes", "puck_last_error")
 
 _lib = None
 _lock = threading.Lock()
@@ -126,6 +126,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_server_get_stats.restype = I
         L.puck_server_pass_ms.argtypes = [P, I, ctypes.POINTER(ctypes.c_double)]
         L.puck_server_pass_ms.restype = I
+        L.puck_server_lanes.argtypes = [P]
+        L.puck_server_lanes.restype = I
         L.puck_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         L.puck_last_error.restype = ctypes.c_size_t
         _lib = L

@@ -1566,6 +1566,7 @@ void puck_default_options(puck_options* o) {
   o->prune_threshold = -9.0f;
   o->use_graphs = 0;
   o->tensor_cores = 0;
+  o->server_lanes = 0;
 }
 
 puck_grammar* puck_grammar_load(const char* path, puck_status* status) {

@@ -218,13 +218,16 @@ struct StepList {
 
 }  // namespace
 
-struct puck_server {
+// One lane of the server: a request loop thread with its own streams, chart
+// arena, slots and tick buffers.  puck_server runs several lanes over one
+// set of device grammar tables; a request stays in the lane it was given to.
+struct Lane {
   const puck_grammar* g = nullptr;
   puck_options opt{};
   int nl = 0;
   bool mbr = false;
   cudaStream_t stream = nullptr, dstream = nullptr;
-  std::vector<std::unique_ptr<LevelDev>> levels;
+  std::vector<std::shared_ptr<LevelDev>> levels;  // shared by the lanes
   std::vector<LevelArena> la;
   DevBuf d_len, d_cell_off, d_node_off, d_mbr_off, d_words, d_status, d_counters, d_decode, d_scratch, d_parts,
       d_cell_cnt;
@@ -240,6 +243,7 @@ struct puck_server {
 
   mutable std::mutex mu;
   std::condition_variable cv_submit, cv_done;
+  std::condition_variable* any_done = nullptr;  // the server's: notified with cv_done
   std::deque<int64_t> pending;
   std::unordered_map<int64_t, Request> reqs;
   std::deque<int64_t> done_q;
@@ -278,7 +282,7 @@ void ensure_out(TickBuf& T, size_t nodes) {
   T.out_cap = want;
 }
 
-int group_of(const puck_server* S, const Resident& r) {
+int group_of(const Lane* S, const Resident& r) {
   return r.stage == ST_DEC ? 4 * S->nl : 4 * r.level + r.stage;
 }
 
@@ -294,7 +298,7 @@ long long units_of(const Resident& r) {
 // Next pass step of a sentence (the order of CLParser.parse for one sentence:
 // per level lexicon, inside spans 1..n, outside spans n..1 where needed,
 // masks; then the decode of the last level).
-void advance(const puck_server* S, Resident& r) {
+void advance(const Lane* S, Resident& r) {
   const LevelArena& A = S->la[r.level];
   switch (r.stage) {
     case ST_LEX: r.stage = ST_IN; r.span = 1; return;
@@ -312,7 +316,7 @@ void advance(const puck_server* S, Resident& r) {
   }
 }
 
-void fail_all(puck_server* S, puck_status st) {
+void fail_all(Lane* S, puck_status st) {
   std::lock_guard<std::mutex> lk(S->mu);
   S->stopping = true;  // the request loop has ended: later submits are refused
   const int64_t t = now_ns();
@@ -334,9 +338,10 @@ void fail_all(puck_server* S, puck_status st) {
   S->resident.clear();
   S->stats.resident = 0;
   S->cv_done.notify_all();
+  if (S->any_done) S->any_done->notify_all();
 }
 
-void harvest(puck_server* S, int p) {
+void harvest(Lane* S, int p) {
   TickBuf& T = S->tb[p];
   CUDA_TRY(cudaEventSynchronize(T.ev_end));
   float ms = 0.f, dms = 0.f;
@@ -367,6 +372,7 @@ void harvest(puck_server* S, int p) {
   S->stats.d2h_bytes += T.d2h;
   T.finishing.clear();
   S->cv_done.notify_all();
+  if (S->any_done) S->any_done->notify_all();
 }
 
 // Launches the coarse levels of one group (the sentences admitted in one
@@ -374,7 +380,7 @@ void harvest(puck_server* S, int p) {
 // have run: per level the lexicon, inside spans 1..n, outside spans n..1 and
 // the masks (and scales for a Real next level), each launch covering every
 // sentence of the group with cells of that span.
-void launch_group(puck_server* S, int gi, const std::vector<std::pair<int, int>>& members, int p) {
+void launch_group(Lane* S, int gi, const std::vector<std::pair<int, int>>& members, int p) {
   CoarseGroup& Gp = S->groups[gi];
   cudaStream_t cs = S->cstream;
   const int ns = (int)members.size();
@@ -483,7 +489,7 @@ void launch_group(puck_server* S, int gi, const std::vector<std::pair<int, int>>
 
 // Builds, uploads and launches one tick into buffer p.  Returns false when
 // nothing was resident.
-bool run_tick(puck_server* S, int p) {
+bool run_tick(Lane* S, int p) {
   TickBuf& T = S->tb[p];
   T.launches = T.h2d = T.d2h = 0;
   std::vector<SlotUpdate> upd;
@@ -801,7 +807,7 @@ bool run_tick(puck_server* S, int p) {
   return true;
 }
 
-void loop_main(puck_server* S) {
+void loop_main(Lane* S) {
   try {
     CUDA_TRY(cudaSetDevice(S->opt.device));
     std::deque<int> inflight;
@@ -839,7 +845,7 @@ void loop_main(puck_server* S) {
   }
 }
 
-int64_t server_bytes_per_cell(const puck_server* S) {
+int64_t server_bytes_per_cell(const Lane* S) {
   int64_t b = 8;  // the sentence's words at its first cells; the cell's part counter
   for (int l = 0; l < S->nl; ++l) {
     const HostLevel& L = S->g->levels[l];
@@ -853,7 +859,7 @@ int64_t server_bytes_per_cell(const puck_server* S) {
   return b;
 }
 
-void destroy_server(puck_server* S) {
+void destroy_server(Lane* S) {
   cudaSetDevice(S->opt.device);
   for (TickBuf& T : S->tb) {
     if (T.host) cudaFreeHost(T.host);
@@ -887,19 +893,15 @@ void destroy_server(puck_server* S) {
   delete S;
 }
 
-}  // namespace
-
-extern "C" {
-
-int64_t puck_server_now_ns(void) { return now_ns(); }
-
-puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts, puck_status* status) {
-  auto* S = new puck_server();
+// A lane over the server's device grammar tables; opt holds the lane's share
+// of the memory budget (mem_bytes) and of the slots (max_batch_sentences).
+Lane* lane_create(const puck_grammar* g, const puck_options& opt, const std::vector<std::shared_ptr<LevelDev>>& levels,
+                  std::condition_variable* any_done, puck_status* status) {
+  auto* S = new Lane();
   try {
-    if (!g) throw PuckError{PUCK_ERR_INVALID_ARG, "null grammar"};
     S->g = g;
-    if (opts) S->opt = *opts;
-    else puck_default_options(&S->opt);
+    S->opt = opt;
+    S->any_done = any_done;
     if (S->opt.max_length <= 0) S->opt.max_length = 100;
     if (S->opt.max_length > puck::kMaxLen)
       throw PuckError{PUCK_ERR_INVALID_ARG, "max_length above " + std::to_string(puck::kMaxLen)};
@@ -941,10 +943,7 @@ puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts,
       T.ev_group.resize(4 * S->nl + 1);
       for (cudaEvent_t& e : T.ev_group) CUDA_TRY(cudaEventCreate(&e));
     }
-    for (int l = 0; l < S->nl; ++l) {
-      S->levels.emplace_back(new LevelDev());
-      build_level(*S->levels.back(), g->levels[l], l < S->nl - 1 && S->nl != 1);
-    }
+    S->levels = levels;
     S->la.resize(S->nl);
     for (int l = 0; l < S->nl; ++l) {
       LevelArena& A = S->la[l];
@@ -1009,7 +1008,7 @@ puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts,
   return nullptr;
 }
 
-void puck_server_destroy(puck_server* S) {
+void lane_destroy(Lane* S) {
   if (!S) return;
   {
     std::lock_guard<std::mutex> lk(S->mu);
@@ -1020,12 +1019,10 @@ void puck_server_destroy(puck_server* S) {
   destroy_server(S);
 }
 
-puck_status puck_server_submit(puck_server* S, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
-                               const int64_t* arrival_ns, int64_t* ids) {
-  if (!S || nsent < 0 || (nsent > 0 && (!word_ids || !offsets || !ids))) {
-    puck::set_last_error("puck_server_submit: null argument or negative count");
-    return PUCK_ERR_INVALID_ARG;
-  }
+// Queues sentences i = 0..nsent-1 in this lane; ids[i] receives the lane's
+// id of each.
+puck_status lane_submit(Lane* S, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                        const int64_t* arrival_ns, int64_t* ids) {
   const int64_t t = now_ns();
   const int nwords = S->g->levels.back().n_words;
   const long long cap = S->arena.cap();
@@ -1064,11 +1061,12 @@ puck_status puck_server_submit(puck_server* S, const int32_t* word_ids, const in
   }
   S->cv_submit.notify_all();
   S->cv_done.notify_all();
+  if (S->any_done) S->any_done->notify_all();
   return PUCK_OK;
 }
 
-int32_t puck_server_poll(puck_server* S, int64_t* ids, int32_t max_ids, int32_t wait_ms) {
-  if (!S || !ids || max_ids <= 0) return 0;
+int32_t lane_poll(Lane* S, int64_t* ids, int32_t max_ids, int32_t wait_ms) {
+  if (max_ids <= 0) return 0;
   std::unique_lock<std::mutex> lk(S->mu);
   if (S->done_q.empty() && wait_ms > 0)
     S->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !S->done_q.empty(); });
@@ -1080,9 +1078,8 @@ int32_t puck_server_poll(puck_server* S, int64_t* ids, int32_t max_ids, int32_t 
   return k;
 }
 
-puck_status puck_server_take(puck_server* S, int64_t id, puck_tree_node* nodes, int32_t max_nodes,
-                             int32_t* sent_status, int64_t* latency_ns) {
-  if (!S) return PUCK_ERR_INVALID_ARG;
+puck_status lane_take(Lane* S, int64_t id, puck_tree_node* nodes, int32_t max_nodes, int32_t* sent_status,
+                      int64_t* latency_ns) {
   std::lock_guard<std::mutex> lk(S->mu);
   auto it = S->reqs.find(id);
   if (it == S->reqs.end() || it->second.t_done == 0) {
@@ -1101,18 +1098,227 @@ puck_status puck_server_take(puck_server* S, int64_t id, puck_tree_node* nodes, 
   return PUCK_OK;
 }
 
+puck_server_stats lane_stats(const Lane* S) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  return S->stats;
+}
+
+void lane_pass_ms(const Lane* S, int32_t level, double out[5]) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  for (int k = 0; k < 5; ++k) out[k] += S->pass_ms[level][k];
+}
+
+}  // namespace
+
+// The server: lanes over one set of device grammar tables.  A request goes to
+// the lane with the fewest cells queued or resident (ties: the lower lane);
+// its id is the lane's id times the lane count plus the lane.  Each lane runs
+// its own ticks on its own streams, so the tail of one lane's launches
+// overlaps the other lanes' work instead of idling the GPU.
+struct puck_server {
+  std::vector<std::shared_ptr<LevelDev>> levels;
+  std::vector<Lane*> lanes;
+  std::vector<int64_t> load;  // per lane: cells of its submitted requests not yet taken
+  std::unordered_map<int64_t, int64_t> cells_of;  // request id -> its cells (until taken)
+  int nl = 0;
+  std::mutex mu;
+  std::condition_variable done;  // some lane finished a request
+};
+
+namespace {
+
+// Lanes for a server: opts->server_lanes (0: two), fewer when a lane's share
+// of the memory budget or of the slots would be too small for a sentence of
+// the maximum length or for a useful batch.
+int lane_count(const puck_options& o, int64_t budget, int64_t per_cell) {
+  int lanes = o.server_lanes > 0 ? o.server_lanes : 2;
+  lanes = std::min(lanes, 8);
+  const int64_t maxlen = o.max_length > 0 ? o.max_length : 100;
+  while (lanes > 1 && (budget / lanes) / std::max<int64_t>(per_cell, 1) < 8 * tri(maxlen)) --lanes;
+  if (o.max_batch_sentences > 0) lanes = std::max(1, std::min(lanes, o.max_batch_sentences / 16));
+  return lanes;
+}
+
+void destroy_all(puck_server* S) {
+  for (Lane* L : S->lanes) lane_destroy(L);
+  S->lanes.clear();
+  S->levels.clear();
+  delete S;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t puck_server_now_ns(void) { return now_ns(); }
+
+puck_server* puck_server_create(const puck_grammar* g, const puck_options* opts, puck_status* status) {
+  auto* S = new puck_server();
+  try {
+    if (!g) throw PuckError{PUCK_ERR_INVALID_ARG, "null grammar"};
+    puck_options o;
+    if (opts) o = *opts;
+    else puck_default_options(&o);
+    S->nl = (int)g->levels.size();
+    if (S->nl < 1 || S->nl > kMaxLevels) throw PuckError{PUCK_ERR_INVALID_ARG, "unsupported number of levels"};
+    int ndev = 0;
+    CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (o.device < 0 || o.device >= ndev) throw PuckError{PUCK_ERR_INVALID_ARG, "no such CUDA device"};
+    CUDA_TRY(cudaSetDevice(o.device));
+    for (int l = 0; l < S->nl; ++l) {
+      S->levels.emplace_back(new LevelDev());
+      build_level(*S->levels.back(), g->levels[l], l < S->nl - 1 && S->nl != 1);
+    }
+    size_t free_b = 0, total_b = 0;
+    CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+    const int64_t cap = (int64_t)(free_b * 0.8);
+    const int64_t budget = o.mem_bytes > 0 ? std::min<int64_t>(o.mem_bytes, cap) : cap;
+    int64_t per_cell = 8;
+    for (const HostLevel& L : g->levels) per_cell += (int64_t)(L.cell_size + 2 * L.mask_size) * 8;
+    const int n = lane_count(o, budget, per_cell);
+    puck_options lo = o;
+    lo.mem_bytes = budget / n;
+    if (o.max_batch_sentences > 0) lo.max_batch_sentences = std::max(1, o.max_batch_sentences / n);
+    for (int k = 0; k < n; ++k) {
+      puck_status st = PUCK_OK;
+      Lane* L = lane_create(g, lo, S->levels, &S->done, &st);
+      if (!L) {
+        char msg[512];
+        puck_last_error(msg, sizeof msg);
+        throw PuckError{st, msg};
+      }
+      S->lanes.push_back(L);
+    }
+    S->load.assign(n, 0);
+    if (status) *status = PUCK_OK;
+    return S;
+  } catch (const PuckError& e) {
+    puck::set_last_error(e.msg);
+    if (status) *status = e.status;
+  }
+  destroy_all(S);
+  return nullptr;
+}
+
+void puck_server_destroy(puck_server* S) {
+  if (!S) return;
+  destroy_all(S);
+}
+
+puck_status puck_server_submit(puck_server* S, const int32_t* word_ids, const int64_t* offsets, int32_t nsent,
+                               const int64_t* arrival_ns, int64_t* ids) {
+  if (!S || nsent < 0 || (nsent > 0 && (!word_ids || !offsets || !ids))) {
+    puck::set_last_error("puck_server_submit: null argument or negative count");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  const int nlanes = (int)S->lanes.size();
+  const int64_t t = now_ns();
+  std::lock_guard<std::mutex> lk(S->mu);
+  // each sentence to the least-loaded lane, then one submit per lane in order
+  std::vector<std::vector<int>> pick(nlanes);
+  std::vector<int64_t> cells(nsent);
+  for (int i = 0; i < nsent; ++i) {
+    const int64_t len = std::max<int64_t>(offsets[i + 1] - offsets[i], 0);
+    cells[i] = 2 * tri(len);
+    int best = 0;
+    for (int k = 1; k < nlanes; ++k)
+      if (S->load[k] < S->load[best]) best = k;
+    S->load[best] += cells[i];
+    pick[best].push_back(i);
+  }
+  std::vector<int32_t> w;
+  std::vector<int64_t> off, arr, lid;
+  for (int k = 0; k < nlanes; ++k) {
+    if (pick[k].empty()) continue;
+    w.clear();
+    off.assign(1, 0);
+    arr.clear();
+    for (int i : pick[k]) {
+      w.insert(w.end(), word_ids + offsets[i], word_ids + std::max(offsets[i], offsets[i + 1]));
+      off.push_back((int64_t)w.size());
+      arr.push_back(arrival_ns && arrival_ns[i] > 0 ? arrival_ns[i] : t);
+    }
+    lid.assign(pick[k].size(), 0);
+    const puck_status st = lane_submit(S->lanes[k], w.data(), off.data(), (int32_t)pick[k].size(), arr.data(),
+                                       lid.data());
+    if (st != PUCK_OK) return st;
+    for (size_t q = 0; q < pick[k].size(); ++q) {
+      const int64_t id = lid[q] * nlanes + k;
+      ids[pick[k][q]] = id;
+      S->cells_of[id] = cells[pick[k][q]];
+    }
+  }
+  return PUCK_OK;
+}
+
+int32_t puck_server_poll(puck_server* S, int64_t* ids, int32_t max_ids, int32_t wait_ms) {
+  if (!S || !ids || max_ids <= 0) return 0;
+  const int nlanes = (int)S->lanes.size();
+  const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(std::max(wait_ms, 0));
+  for (;;) {
+    int32_t k = 0;
+    for (int l = 0; l < nlanes && k < max_ids; ++l) {
+      const int32_t got = lane_poll(S->lanes[l], ids + k, max_ids - k, 0);
+      for (int32_t q = k; q < k + got; ++q) ids[q] = ids[q] * nlanes + l;
+      k += got;
+    }
+    if (k > 0 || std::chrono::steady_clock::now() >= deadline) return k;
+    // a lane notifies `done` when it finishes a request; the short timeout
+    // covers a notification between the polls above and this wait
+    std::unique_lock<std::mutex> lk(S->mu);
+    S->done.wait_until(lk, std::min(deadline, std::chrono::steady_clock::now() + std::chrono::milliseconds(1)));
+  }
+}
+
+puck_status puck_server_take(puck_server* S, int64_t id, puck_tree_node* nodes, int32_t max_nodes,
+                             int32_t* sent_status, int64_t* latency_ns) {
+  if (!S || id < 0) {
+    puck::set_last_error("puck_server_take: no finished request with this id");
+    return PUCK_ERR_INVALID_ARG;
+  }
+  const int nlanes = (int)S->lanes.size();
+  const int l = (int)(id % nlanes);
+  const puck_status st = lane_take(S->lanes[l], id / nlanes, nodes, max_nodes, sent_status, latency_ns);
+  if (st == PUCK_OK) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->cells_of.find(id);
+    if (it != S->cells_of.end()) {
+      S->load[l] -= it->second;
+      S->cells_of.erase(it);
+    }
+  }
+  return st;
+}
+
 puck_status puck_server_get_stats(const puck_server* S, puck_server_stats* out) {
   if (!S || !out) return PUCK_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(S->mu);
-  *out = S->stats;
+  puck_server_stats sum{};
+  for (const Lane* L : S->lanes) {
+    const puck_server_stats s = lane_stats(L);
+    sum.submitted += s.submitted;
+    sum.completed += s.completed;
+    sum.failed += s.failed;
+    sum.ticks += s.ticks;
+    sum.kernel_launches += s.kernel_launches;
+    sum.resident += s.resident;
+    sum.resident_peak += s.resident_peak;
+    sum.arena_cells += s.arena_cells;
+    sum.arena_cells_peak += s.arena_cells_peak;
+    sum.ms_device += s.ms_device;
+    sum.h2d_bytes += s.h2d_bytes;
+    sum.d2h_bytes += s.d2h_bytes;
+  }
+  *out = sum;
   return PUCK_OK;
 }
 
 puck_status puck_server_pass_ms(const puck_server* S, int32_t level, double out[5]) {
   if (!S || !out || level < 0 || level >= S->nl) return PUCK_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lk(S->mu);
-  for (int k = 0; k < 5; ++k) out[k] = S->pass_ms[level][k];
+  for (int k = 0; k < 5; ++k) out[k] = 0.0;
+  for (const Lane* L : S->lanes) lane_pass_ms(L, level, out);
   return PUCK_OK;
 }
+
+int32_t puck_server_lanes(const puck_server* S) { return S ? (int32_t)S->lanes.size() : 0; }
 
 }  // extern "C"

@@ -34,10 +34,11 @@ class CLServer:
 
     def __init__(self, grammar_path: str, max_alloc_size: int = 1 << 30, device: int = 0,
                  decode: str = "auto", max_length: int = 100, prune_threshold: float = -9.0,
-                 max_resident: int = 0, collect: bool = True, profile: bool = False):
+                 max_resident: int = 0, collect: bool = True, profile: bool = False, lanes: int = 0):
         """collect=True starts a thread that takes finished requests and
         completes their futures; with collect=False the caller drives
-        ``poll``/``take`` itself."""
+        ``poll``/``take`` itself.  lanes: independent request loops (0: the
+        library's default)."""
         L = _lib.load()
         self._L = L
         st = ctypes.c_int32(0)
@@ -54,6 +55,7 @@ class CLServer:
         opt.prune_threshold = prune_threshold
         opt.max_batch_sentences = max_resident
         opt.profile = 1 if profile else 0
+        opt.server_lanes = lanes
         self._s = L.puck_server_create(self._g, ctypes.byref(opt), ctypes.byref(st))
         if not self._s:
             err = _lib.last_error()
@@ -93,6 +95,10 @@ class CLServer:
         _lib.check(self._L.puck_server_take(self._s, int(rid), nodes.ctypes.data, nodes.shape[0],
                                             ctypes.byref(st), ctypes.byref(lat)))
         return nodes[:max(2 * n - 1, 0)], int(st.value), int(lat.value)
+
+    def lanes(self) -> int:
+        """Lanes (independent request loops) the server runs."""
+        return int(self._L.puck_server_lanes(self._s))
 
     def stats(self) -> dict:
         s = _lib.ServerStats()

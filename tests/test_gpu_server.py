@@ -82,6 +82,27 @@ def test_server_viterbi_same_alone_and_in_mix_and_oracle():
     assert st["resident_peak"] > 1  # sentences shared the GPU
 
 
+@pytest.mark.parametrize("lanes", [1, 3])
+def test_server_lanes_match_oracle(lanes):
+    """One lane, or three independent request loops sharing the GPU: every
+    served tree equals the oracle's whatever lane it ran in."""
+    levels = split_levels("viterbi", "medium")
+    path = write_grz(levels, "split_medium")
+    sents = split_sentences(45, seed=29, mean=16, hi=40)
+    r = oracle.run(levels, sents, mode="parse")
+    ref = node_blocks(r.trees(), [len(s) for s in sents])
+    S = CLServer(path, max_alloc_size=2 << 30, collect=False, lanes=lanes)
+    try:
+        assert S.lanes() == lanes
+        served = _serve_mix(S, sents, gap_s=0.0005, chunk=5)
+        st = S.stats()
+    finally:
+        S.close()
+    for i, blk in enumerate(served):
+        assert np.array_equal(blk, ref[i]), i
+    assert st["completed"] == len(sents) and st["failed"] == 0
+
+
 def test_server_lengths_to_60_match_oracle_and_batch():
     """The serving lengths (lognormal mean 23 clipped 1-60) with several
     sentences of 41-60 words: each served tree equals the oracle's and the

@@ -29,15 +29,19 @@ def test_library_exports_every_declared_symbol():
 
 
 def test_options_layout_and_defaults():
-    """The ctypes mirror of puck_options has the C layout (40 bytes, no
-    padding after tensor_cores) and the library's defaults."""
+    """The ctypes mirror of puck_options has the C layout (48 bytes:
+    server_lanes at 40, then padding to the int64 alignment) and the
+    library's defaults."""
     L = _lib.load()
-    assert ctypes.sizeof(_lib.Options) == 40
+    assert ctypes.sizeof(_lib.Options) == 48
     assert _lib.Options.tensor_cores.offset == 36
+    assert _lib.Options.server_lanes.offset == 40
     opt = _lib.Options()
     opt.tensor_cores = 7
+    opt.server_lanes = 5
     L.puck_default_options(ctypes.byref(opt))
     assert opt.tensor_cores == 0 and opt.use_graphs == 0 and abs(opt.prune_threshold + 9.0) < 1e-6
+    assert opt.server_lanes == 0
 
 
 def test_tc_selftest_rejects_bad_shapes_without_a_device_call():
