@@ -147,7 +147,12 @@ struct Request {
 
 enum Stage { ST_LEX = 0, ST_IN = 1, ST_OUT = 2, ST_MASK = 3, ST_DEC = 4, ST_WAIT = 5 };
 
-constexpr int kGroups = 8;  // coarse groups in flight
+// Coarse groups in flight per lane.  Admission waits while both are busy, so
+// under load the next group gathers more sentences and its coarse batch
+// runs larger launches (two in flight against eight: at 6,000 sentences/s
+// offered p50 latency 85 against 165 ms, and 5% more sentences/s at
+// saturation on the C1 grammar).
+constexpr int kGroups = 2;
 
 // A resident sentence and its pass cursor (owned by the loop thread).
 struct Resident {
