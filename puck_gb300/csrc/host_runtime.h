@@ -75,7 +75,8 @@ struct LevelDev {
   puck::DevLevel d{};
   puck::DevTc tc{};
   bool tc_ok = false;     // the tensor-core tables were built
-  bool flat_ready = false;  // every Viterbi inside job has the flat-tile layout (DevJob::flat)
+  bool flat_ready_in = false;   // every inside job with rules has the flat-tile layout (DevJob::flat)
+  bool flat_ready_out = false;  // every outside job with rules has it
   std::string tc_why;     // else why not
   void* upload(const void* src, size_t bytes) {
     void* p = nullptr;

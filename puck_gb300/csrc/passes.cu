@@ -85,17 +85,18 @@ struct Smem {
 };
 
 // Floats of each warp's outer-product tile: the flat-tile sub-tiles (at most
-// 16 x 16) in the Viterbi inside kernel of a level whose inside jobs are all
-// flat, else the level's largest pair.
-__host__ __device__ __forceinline__ int mtile_floats(const DevLevel& L, bool with_stage) {
-  return with_stage && L.flat_inside ? L.flat_mtile : L.max_mtile;
+// 16 x 16) in a flat-tile kernel (MODE 3), else the level's largest pair.
+__host__ __device__ __forceinline__ int mtile_floats(const DevLevel& L, bool flat) {
+  return flat ? L.flat_mtile : L.max_mtile;
 }
 
-// with_stage: the per-warp operand stage of the Viterbi inside pass;
-// pairs: a pair-factored kernel (MODE 2 or 3; the outside kernel tests the
-// level's mode at run time instead, which keeps its target-major register
-// allocation free of spills)
-__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage, bool pairs) {
+// with_stage: the per-warp operand stage (the Viterbi inside pass and the
+// flat-tile kernels); pairs: a pair-factored kernel (MODE 2 or 3; the outside
+// kernel tests the level's mode at run time instead, which keeps its
+// target-major register allocation free of spills); flat: a flat-tile kernel
+// (MODE 3)
+__device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk, bool with_stage, bool pairs,
+                                      bool flat) {
   Smem m;
   const int cs = L.cell_size;
   m.P = base;
@@ -105,7 +106,7 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
   m.pl = nullptr;
   m.list = nullptr;
   m.slist = nullptr;
-  m.mtile = mtile_floats(L, with_stage);
+  m.mtile = mtile_floats(L, flat);
   if (pairs) {
     if (with_stage) {
       m.stage = rest;
@@ -258,14 +259,27 @@ __device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned lon
 // This lane's operand value for each of the four splits of group g (see
 // grid_outer): one 4-byte load fetches the group's split positions from the
 // warp's live-split list, then their row pointers.
-__device__ __forceinline__ float4 load_group(const float* const* rows, const unsigned char* sl, int g, unsigned src,
-                                             bool ok) {
+// Sum-product: the positions past the pair's n live splits (the list's
+// repeats) add nothing, and the left operand (scl != nullptr) carries each
+// split's scale.
+template <int S>
+__device__ __forceinline__ float4 load_group(const float* const* rows, const float* scl, const unsigned char* sl,
+                                             int g, unsigned src, bool ok, int n) {
   const unsigned q = *reinterpret_cast<const unsigned*>(sl + 4 * g);
+  const unsigned i0 = q & 255u, i1 = (q >> 8) & 255u, i2 = (q >> 16) & 255u, i3 = q >> 24;
   float4 v;
-  v.x = ok ? __ldg(rows[q & 255u] + src) : -CUDART_INF_F;
-  v.y = ok ? __ldg(rows[(q >> 8) & 255u] + src) : -CUDART_INF_F;
-  v.z = ok ? __ldg(rows[(q >> 16) & 255u] + src) : -CUDART_INF_F;
-  v.w = ok ? __ldg(rows[q >> 24] + src) : -CUDART_INF_F;
+  if (S == SEMI_VITERBI) {
+    v.x = ok ? __ldg(rows[i0] + src) : -CUDART_INF_F;
+    v.y = ok ? __ldg(rows[i1] + src) : -CUDART_INF_F;
+    v.z = ok ? __ldg(rows[i2] + src) : -CUDART_INF_F;
+    v.w = ok ? __ldg(rows[i3] + src) : -CUDART_INF_F;
+  } else {
+    const int b = 4 * g;
+    v.x = ok && b < n ? __ldg(rows[i0] + src) * (scl ? scl[i0] : 1.f) : 0.f;
+    v.y = ok && b + 1 < n ? __ldg(rows[i1] + src) * (scl ? scl[i1] : 1.f) : 0.f;
+    v.z = ok && b + 2 < n ? __ldg(rows[i2] + src) * (scl ? scl[i2] : 1.f) : 0.f;
+    v.w = ok && b + 3 < n ? __ldg(rows[i3] + src) * (scl ? scl[i3] : 1.f) : 0.f;
+  }
   return v;
 }
 
@@ -282,7 +296,10 @@ __device__ __forceinline__ float4 load_group(const float* const* rows, const uns
 // 3-input maxes.  The operand loads of the next group are issued before the
 // current group's arithmetic, into the other of the warp's two stage buffers.
 // Rows past the tile read the -inf rows; their entries are not stored.
-template <int RJ, int RK>
+// Sum-product: M[j * nz + k] = sum over the live splits of scale_s A_s[Y_j]
+// B_s[Z_k], four fused multiply-adds per entry and group, the scale applied
+// to A when it is staged.
+template <int S, int RJ, int RK>
 __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsigned char* sl, int n, int4 D,
                                            float4* st4, float* Mw) {
   const int lane = threadIdx.x & 31;
@@ -297,15 +314,16 @@ __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsig
 #pragma unroll
   for (int a = 0; a < RJ; ++a)
 #pragma unroll
-    for (int b = 0; b < RK; ++b) acc[a][b] = -CUDART_INF_F;
+    for (int b = 0; b < RK; ++b) acc[a][b] = Sr<S>::zero();
   const bool a_side = lane < 16;
   const int mem = a_side ? lane : lane - 16;
   const bool ok = mem < (a_side ? ny : nz);
   const unsigned src = (a_side ? (unsigned)D.x & 0xffffu : (unsigned)D.x >> 16) + mem;
   const float* const* rows = (a_side ? X.aptr : X.bptr) + c0;
+  const float* scl = S == SEMI_REAL && a_side ? X.scl + c0 : nullptr;
   const int my_row = a_side ? mem : kStageRowB + mem;
   int g = 0;
-  float4 v = load_group(rows, sl, 0, src, ok);
+  float4 v = load_group<S>(rows, scl, sl, 0, src, ok, n);
   for (int buf = 0;; buf ^= 1) {
     float4* sb = st4 + buf * kStageRows;
     sb[my_row] = v;
@@ -313,7 +331,7 @@ __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsig
     const bool rest = 4 * (g + 1) < n;
     if (rest) {
       ++g;
-      v = load_group(rows, sl, g, src, ok);
+      v = load_group<S>(rows, scl, sl, g, src, ok, n);
     }
     const char* stb = reinterpret_cast<const char*>(sb);
     float4 A[RJ];
@@ -324,10 +342,17 @@ __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsig
       const float4 B = *reinterpret_cast<const float4*>(stb + offB[b]);
 #pragma unroll
       for (int a = 0; a < RJ; ++a) {
-        const float2 t01 = add2(make_float2(A[a].x, A[a].y), make_float2(B.x, B.y));
-        const float2 t23 = add2(make_float2(A[a].z, A[a].w), make_float2(B.z, B.w));
-        acc[a][b] = max3(acc[a][b], t01.x, t01.y);
-        acc[a][b] = max3(acc[a][b], t23.x, t23.y);
+        if (S == SEMI_VITERBI) {
+          const float2 t01 = add2(make_float2(A[a].x, A[a].y), make_float2(B.x, B.y));
+          const float2 t23 = add2(make_float2(A[a].z, A[a].w), make_float2(B.z, B.w));
+          acc[a][b] = max3(acc[a][b], t01.x, t01.y);
+          acc[a][b] = max3(acc[a][b], t23.x, t23.y);
+        } else {
+          acc[a][b] = fmaf(A[a].x, B.x, acc[a][b]);
+          acc[a][b] = fmaf(A[a].y, B.y, acc[a][b]);
+          acc[a][b] = fmaf(A[a].z, B.z, acc[a][b]);
+          acc[a][b] = fmaf(A[a].w, B.w, acc[a][b]);
+        }
       }
     }
     if (!rest) break;
@@ -342,8 +367,11 @@ __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsig
 
 // The gated-in blocks of one flat-tile pair: each lane runs its one-target
 // slice four rules per record, fl(M[e] + w) folded with packed adds and
-// 3-input maxes, and flushes once per block.  A block's descriptor
-// {segment, first record, end record, rules} is read one block ahead.
+// 3-input maxes (sum-product: M[e] w summed with fused multiply-adds; a
+// padding rule, weight 0, adds nothing even where M[e] overflowed), and
+// flushes once per block.  A block's descriptor {segment, first record, end
+// record, rules} is read one block ahead.
+template <int S>
 __device__ __forceinline__ void flat_rules(const DevJob& J, const CellCtx& X, int4 D, const float* Mw, float* P,
                                            unsigned long long& work, unsigned long long& corner) {
   const int lane = threadIdx.x & 31;
@@ -354,17 +382,24 @@ __device__ __forceinline__ void flat_rules(const DevJob& J, const CellCtx& X, in
     if (q + 1 < nb) nxt = __ldg(J.fr_blk + b0 + q + 1);
     if (!((X.segpass[B.x >> 5] >> (B.x & 31)) & 1u)) continue;
     const int t = __ldg(J.fr_tgt + (b0 + q) * 32 + lane);
-    float best = -CUDART_INF_F;
+    float best = Sr<S>::zero();
 #pragma unroll 2
     for (int g = B.y + lane; g < B.z; g += 32) {
       const unsigned o = __ldg(J.fr_idx + g);
       const float4 w = __ldg(J.fr_w + g);
-      const float2 t01 = add2(make_float2(Mw[o & 255u], Mw[(o >> 8) & 255u]), make_float2(w.x, w.y));
-      const float2 t23 = add2(make_float2(Mw[(o >> 16) & 255u], Mw[o >> 24]), make_float2(w.z, w.w));
-      best = max3(best, t01.x, t01.y);
-      best = max3(best, t23.x, t23.y);
+      if (S == SEMI_VITERBI) {
+        const float2 t01 = add2(make_float2(Mw[o & 255u], Mw[(o >> 8) & 255u]), make_float2(w.x, w.y));
+        const float2 t23 = add2(make_float2(Mw[(o >> 16) & 255u], Mw[o >> 24]), make_float2(w.z, w.w));
+        best = max3(best, t01.x, t01.y);
+        best = max3(best, t23.x, t23.y);
+      } else {
+        best = fmaf(w.x != 0.f ? Mw[o & 255u] : 0.f, w.x, best);
+        best = fmaf(w.y != 0.f ? Mw[(o >> 8) & 255u] : 0.f, w.y, best);
+        best = fmaf(w.z != 0.f ? Mw[(o >> 16) & 255u] : 0.f, w.z, best);
+        best = fmaf(w.w != 0.f ? Mw[o >> 24] : 0.f, w.w, best);
+      }
     }
-    if (t >= 0) flush_run<SEMI_VITERBI>(P, t, best, corner);
+    if (t >= 0) flush_run<S>(P, t, best, corner);
     if (lane == 0) work += (unsigned long long)B.w;
   }
   __syncwarp();
@@ -373,6 +408,7 @@ __device__ __forceinline__ void flat_rules(const DevJob& J, const CellCtx& X, in
 // The live pairs of a flat-tile job for one chunk of splits.  Warps take
 // pairs from a shared counter (this part's pairs are list positions g,
 // g + G, g + 2G, ...), so a warp that drew cheap pairs takes more of them.
+template <int S>
 __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, CellCtx& X, int c0, int nc, int nlive,
                                            int grp, float* Mw, float* P, unsigned long long& work,
                                            unsigned long long& corner) {
@@ -402,15 +438,15 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
     const int ny = D.z & 255, nz = (D.z >> 8) & 255, E = ny * nz;
     const int shape = (ny > 8 ? 3 : 0) + (nz > 12 ? 2 : nz > 8 ? 1 : 0);  // RJ in {1, 2} x RK in {2, 3, 4}
     switch (shape) {
-      case 0: grid_outer<1, 2>(X, c0, sl, n, D, st4, Mw); break;
-      case 1: grid_outer<1, 3>(X, c0, sl, n, D, st4, Mw); break;
-      case 2: grid_outer<1, 4>(X, c0, sl, n, D, st4, Mw); break;
-      case 3: grid_outer<2, 2>(X, c0, sl, n, D, st4, Mw); break;
-      case 4: grid_outer<2, 3>(X, c0, sl, n, D, st4, Mw); break;
-      default: grid_outer<2, 4>(X, c0, sl, n, D, st4, Mw); break;
+      case 0: grid_outer<S, 1, 2>(X, c0, sl, n, D, st4, Mw); break;
+      case 1: grid_outer<S, 1, 3>(X, c0, sl, n, D, st4, Mw); break;
+      case 2: grid_outer<S, 1, 4>(X, c0, sl, n, D, st4, Mw); break;
+      case 3: grid_outer<S, 2, 2>(X, c0, sl, n, D, st4, Mw); break;
+      case 4: grid_outer<S, 2, 3>(X, c0, sl, n, D, st4, Mw); break;
+      default: grid_outer<S, 2, 4>(X, c0, sl, n, D, st4, Mw); break;
     }
     if (lane == 0) work += (unsigned long long)__popcll(m) * E;
-    flat_rules(J, X, D, Mw, P, work, corner);
+    flat_rules<S>(J, X, D, Mw, P, work, corner);
   }
 }
 
@@ -513,7 +549,7 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
     __syncthreads();
     const int nlive = X.nlive;
     if (FLAT) {
-      flat_pairs(J, sm, X, c0, nc, nlive, grp, Mw, P, work, corner);
+      flat_pairs<S>(J, sm, X, c0, nc, nlive, grp, Mw, P, work, corner);
       __syncthreads();
       continue;
     }
@@ -759,8 +795,8 @@ __device__ void gather_pairs(const DevJob& J, const DevLevel& L, bool gated, flo
 template <int S, int MODE>
 __device__ __forceinline__ void gather(const DevJob& J, const DevLevel& L, bool gated, float* P, const Smem& sm,
                                        int chunk, CellCtx& X) {
-  if (MODE == 3) gather_pairs<S, true>(J, L, gated, P, sm, X);
-  else if (MODE == 2 && S != SEMI_LOGSUM) gather_pairs<S>(J, L, gated, P, sm, X);
+  if constexpr (MODE == 3) gather_pairs<S, true>(J, L, gated, P, sm, X);
+  else if constexpr (MODE == 2 && S != SEMI_LOGSUM) gather_pairs<S>(J, L, gated, P, sm, X);
   else gather_targets<S>(J, L, gated, P, sm.stA, sm.stB, chunk, X);
 }
 
@@ -862,14 +898,16 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 // Inside pass over the cells of a work list (span 1: the unary layer over
 // lexicon cells).  Register budgets: five CTAs per SM for the pair-factored
 // passes (48 registers: the flat-tile path keeps up to eight tile entries
-// and their stage offsets in registers), six for the target-major ones.
+// and their stage offsets in registers), four for the sum-product flat-tile
+// pass (its staged loads also carry each split's scale: 80 spilled bytes at
+// 48 registers, none at 64), six for the target-major ones.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
+__global__ void __launch_bounds__(256, MODE == 3 && S == SEMI_REAL ? 4 : MODE >= 2 ? 5 : 6)
     k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk, S == SEMI_VITERBI, MODE >= 2);
+  const Smem sm = carve(smem, L, chunk, S == SEMI_VITERBI || MODE == 3, MODE >= 2, MODE == 3);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -964,13 +1002,13 @@ __global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
 // 64 on the bench's coarse level despite a few spilled bytes), four for the
 // target-major sum-product passes.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE == 2 ? 5 : S == SEMI_VITERBI ? 6 : 4)
+__global__ void __launch_bounds__(256, MODE >= 2 ? 5 : S == SEMI_VITERBI ? 6 : 4)
     k_outside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, const float* inside, float* outside, DevLive V,
                    Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
   const int cs = L.cell_size, ms = L.mask_size;
-  const Smem sm = carve(smem, L, chunk, false, MODE == 3 || L.mode == 2);
+  const Smem sm = carve(smem, L, chunk, MODE == 3, MODE == 3 || L.mode == 2, MODE == 3);
   float* P = sm.P;
   float* Q = sm.Q;
   const int ent = entry_of(W, blockIdx.x);
@@ -1188,10 +1226,10 @@ cudaError_t set_smem(K kernel, size_t bytes) {
 
 }  // namespace
 
-size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs) {
+size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs, bool flat) {
   const size_t cs = L.cell_size;
   if (pairs)
-    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + mtile_floats(L, with_stage))) *
+    return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + mtile_floats(L, flat))) *
                sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int) +
            (with_stage ? (size_t)(kThreads / 32) * kSplitList : 0);
@@ -1230,12 +1268,13 @@ cudaError_t launch_pass(bool inside_pass, const DevLevel& L, const DevBatch& B, 
                         int max_span, const float* inside_c, float* inside, float* outside, DevLive V, Counters C,
                         cudaStream_t st) {
   const int chunk = pick_split_chunk(L.cell_size, max_span);
-  const size_t smem = pass_smem_bytes(L, chunk, inside_pass && S == SEMI_VITERBI, MODE >= 2);
+  const size_t smem =
+      pass_smem_bytes(L, chunk, (inside_pass && S == SEMI_VITERBI) || MODE == 3, MODE >= 2, MODE == 3);
   const unsigned grid = (unsigned)W.nunits;
   if (inside_pass) {
     if (cudaError_t e = set_smem(k_inside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_inside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside, V, C, chunk);
-  } else if constexpr (MODE != 3) {  // the flat-tile form has no outside pass
+  } else {
     if (cudaError_t e = set_smem(k_outside_span<S, MODE>, smem); e != cudaSuccess) return e;
     k_outside_span<S, MODE><<<grid, kThreads, smem, st>>>(L, B, W, M, inside_c, outside, V, C, chunk);
   }
@@ -1249,13 +1288,15 @@ cudaError_t launch_any(bool inside_pass, const DevLevel& L, const DevBatch& B, c
   const bool pairs = L.mode == 2;
   switch (L.semiring) {
     case SEMI_VITERBI:
-      // the flat-tile inside pass (its pairs: of coarse symbols, or of
-      // groups of coarse ids on a target-major level)
-      if (inside_pass && L.flat_inside)
+      // the flat-tile passes (their pairs: of coarse symbols, or of groups
+      // of coarse ids on a target-major level)
+      if (inside_pass ? L.flat_inside : L.flat_outside)
         return launch_pass<SEMI_VITERBI, 3>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
       return pairs ? launch_pass<SEMI_VITERBI, 2>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st)
                    : launch_pass<SEMI_VITERBI, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
     case SEMI_REAL:
+      if (inside_pass ? L.flat_inside : L.flat_outside)
+        return launch_pass<SEMI_REAL, 3>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
       return pairs ? launch_pass<SEMI_REAL, 2>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st)
                    : launch_pass<SEMI_REAL, 0>(inside_pass, L, B, W, M, max_span, inside_c, inside, outside, V, C, st);
     default:

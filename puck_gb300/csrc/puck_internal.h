@@ -86,6 +86,7 @@ struct DevLevel {
   int tc_binary;    // sum-product inside pass: binary sums already in the bot cells (tensor-core form)
   int flat_inside;  // every inside job with rules has the flat-tile layout (DevJob::flat); the
                     // host clears it in its copy of a level for launches of the other form
+  int flat_outside; // the same for the outside jobs
   int flat_mtile;   // largest ny * nz of any flat-tile sub-tile (<= 256); the M tile of the
                     // Viterbi inside kernel when flat_inside
   int pair_group;   // coarse ids per pair key of the flat-tile tables: 1 (pairs of coarse
@@ -224,7 +225,7 @@ cudaError_t launch_mbr_decode(const DevBatch& B, const DevWork& W, const DevMask
 cudaError_t launch_root_scores(const DevLevel& L, const DevBatch& B, const DevWork& W, const DevMask& M,
                                const float* inside, const double* part_scale, float* log_z, cudaStream_t st);
 
-size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs);
+size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs, bool flat);
 
 // Tensor-core inside pass: the binary sums of the cells of one span.  cells
 // holds (sentence, begin) pairs; 128 cells per tile, one CTA per tile and

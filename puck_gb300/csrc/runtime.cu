@@ -304,7 +304,8 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
 // as its gate.  A block with more than 32 targets is cut into runs of 32
 // targets.  Each target of a block gets lanes in proportion to its rule
 // count (at least one); a lane's slice is stored as records of four rules,
-// padded with weight -inf (the max-plus zero, which never changes a cell).
+// padded with weight pad_w (the semiring's zero: -inf for max-plus, 0 for the
+// sum-product, which the kernel skips), which never changes a cell.
 // The sub-tiles form the layout's own pair list (fnpair, fpair_key,
 // fpair_gate).  *mtile receives the largest sub-tile.  Returns false, uploading
 // nothing, when the job does not qualify.
@@ -312,7 +313,7 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
 // operand roles' index spaces) for the left and right operands.
 bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const int* pk, const int* pbk,
                       const int* bs, const int* bp, const int* pr, const float* pw, const int* seg_bits, int nseg,
-                      int ms, const int* ao, const int* am, const int* bo, const int* bm, int* mtile) {
+                      int ms, const int* ao, const int* am, const int* bo, const int* bm, float pad_w, int* mtile) {
   constexpr int kSub = 16;  // largest sub-tile side
   auto contiguous = [](const int* off, const int* mem, int c) {
     for (int i = off[c]; i < off[c + 1]; ++i)
@@ -369,7 +370,7 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
     // reads an entry already read by the slot (weight -inf).
     const size_t base = idx.size();
     idx.resize(base + (size_t)steps * 32, 0u);
-    w.resize(base + (size_t)steps * 32, make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
+    w.resize(base + (size_t)steps * 32, make_float4(pad_w, pad_w, pad_w, pad_w));
     for (int sl = 0; sl < slots; ++sl) {
       int bank_e[32];
       std::fill(bank_e, bank_e + 32, -1);
@@ -404,7 +405,7 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
       for (int l = 0; l < 32; ++l) {
         const size_t at = base + (size_t)(sl / 4) * 32 + l;
         int e = any_e;
-        float wt = -INFINITY;
+        float wt = pad_w;
         if (pick[l] >= 0) {
           e = todo[l][pick[l]].first;
           wt = todo[l][pick[l]].second;
@@ -482,7 +483,7 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
   if (tgt.empty()) tgt.assign(32, -1);
   if (idx.empty()) {
     idx.push_back(0u);
-    w.push_back(make_float4(-INFINITY, -INFINITY, -INFINITY, -INFINITY));
+    w.push_back(make_float4(pad_w, pad_w, pad_w, pad_w));
   }
   J.fpair_key = static_cast<const int*>(D.upload(key.data(), key.size() * sizeof(int)));
   J.fpair_gate = static_cast<const int*>(D.upload(gate.data(), gate.size() * sizeof(int)));
@@ -576,7 +577,7 @@ bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, 
   bp.push_back((int)rs.size());
   return build_flat_tiles(D, J, ntgt, (int64_t)pk.size(), pk.data(), pbk.data(), bs.data(), bp.data(), pr.data(),
                           pw.data(), L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size, ao.data(),
-                          am.data(), bo.data(), bm.data(), mtile);
+                          am.data(), bo.data(), bm.data(), -INFINITY, mtile);
 }
 
 }  // namespace
@@ -762,14 +763,16 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
     J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
-    // Viterbi inside jobs also get the flat-tile layout where it applies
-    if (interleave &&
+    // Viterbi and sum-product jobs (inside and outside) also get the
+    // flat-tile layout where it applies
+    if ((L.semiring == puck::SEMI_VITERBI || L.semiring == puck::SEMI_REAL) &&
         build_flat_tiles(D, J, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw,
                          L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size,
                          L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
                          L.get<int>(a_t[j] ? "t_mem" : "nt_mem", "i4", nullptr),
                          L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
-                         L.get<int>(b_t[j] ? "t_mem" : "nt_mem", "i4", nullptr), &d.flat_mtile))
+                         L.get<int>(b_t[j] ? "t_mem" : "nt_mem", "i4", nullptr),
+                         L.semiring == puck::SEMI_REAL ? 0.f : -INFINITY, &d.flat_mtile))
       d.max_npair = std::max(d.max_npair, J.fnpair);
     J.pair_blk = up<int>(D, L, n + "/pair_blk", "i4");
     J.blk_seg = up<int>(D, L, n + "/blk_seg", "i4");
@@ -786,8 +789,9 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     }
   }
   d.flat_inside = 1;
-  for (int j = puck::IN_NN; j <= puck::IN_TT; ++j)
-    if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0 && !d.jobs[j].flat) d.flat_inside = 0;
+  d.flat_outside = 1;
+  for (int j = 0; j < puck::NJOBS; ++j)
+    if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0 && !d.jobs[j].flat) (j <= puck::IN_TT ? d.flat_inside : d.flat_outside) = 0;
   d.pair_group = 1;
   {
     const int* nn_mode = L.get<int>("in_NN/pair_mode", "i4", nullptr);
@@ -808,11 +812,14 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
       } else {
         d.flat_inside = 0;  // group tables in some jobs, one-symbol pairs in others: not used
       }
+      d.flat_outside = 0;  // its outside jobs keep one-symbol pairs: the target-major scan is faster
     }
-    // The flat-tile inside pass is ready; by default it runs on the
+    // The flat-tile passes are ready; by default they run on the
     // pair-factored levels (the parser's autotuner chooses per span band).
-    D.flat_ready = d.flat_inside != 0;
-    d.flat_inside = D.flat_ready && d.mode == 2;
+    D.flat_ready_in = d.flat_inside != 0;
+    D.flat_ready_out = d.flat_outside != 0;
+    d.flat_inside = D.flat_ready_in && d.mode == 2;
+    d.flat_outside = D.flat_ready_out && d.mode == 2;
     d.nt_mem_off = up<int>(D, L, "nt_mem_off", "i4");
     d.nt_mem = up<int>(D, L, "nt_mem", "i4");
     d.t_mem_off = up<int>(D, L, "t_mem_off", "i4");
@@ -1339,7 +1346,7 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
         } else {
           // the flat-tile form from the level's chosen span on
           puck::DevLevel Ds = D;
-          Ds.flat_inside = P->levels[l]->flat_ready && span >= P->flat_from[l];
+          Ds.flat_inside = P->levels[l]->flat_ready_in && span >= P->flat_from[l];
           CUDA_TRY(puck::launch_inside_span(Ds, B, work(span_list[span], span), MM, max_len, inside, V, C, st));
         }
         ++LC[0];
@@ -1349,7 +1356,9 @@ void run_batch(puck_parser* P, Mode mode, const BatchPlan& plan, const int32_t* 
     if (need_out) {
       launch_sequence(P, l, 1, st, [&] {
         for (int span = max_len; span >= 1; --span) {
-          CUDA_TRY(puck::launch_outside_span(D, B, work(span_list[span], span), MM, max_len, inside, outside, V,
+          puck::DevLevel Ds = D;
+          Ds.flat_outside = P->levels[l]->flat_ready_out && span >= P->flat_from[l];
+          CUDA_TRY(puck::launch_outside_span(Ds, B, work(span_list[span], span), MM, max_len, inside, outside, V,
                                              C, st));
           ++LC[1];
         }
@@ -1639,9 +1648,9 @@ puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts,
       P->levels.emplace_back(new LevelDev());
       LevelDev& LD = *P->levels.back();
       build_level(LD, g->levels[l], l < nl - 1 && nl != 1);
-      // by default the flat-tile inside pass runs at every span of the
-      // pair-factored levels that have it
-      if (LD.d.flat_inside) P->flat_from[l] = 2;
+      // by default the flat-tile passes run at every span of the
+      // pair-factored levels that have them
+      if (LD.d.flat_inside || LD.d.flat_outside) P->flat_from[l] = 2;
       if (P->opt.tensor_cores) {
         if (l == nl - 1) LD.tc_ok = build_tc(LD, g->levels[l], &LD.tc_why);
         else LD.tc_why = "a coarse level of the cascade (it only makes masks)";
@@ -1785,7 +1794,7 @@ puck_status puck_parser_autotune(puck_parser* P, const int32_t* word_ids, const 
   // coarse ids) and the band that keeps the level's own form (the whole
   // pairs' tiles, or one rule at a time): from span 2, 8, 16 or never
   for (int l = 0; l < nl; ++l) {
-    if (!P->levels[l]->flat_ready) continue;
+    if (!P->levels[l]->flat_ready_in && !P->levels[l]->flat_ready_out) continue;
     double best_t = -1.0;
     int best_f = P->flat_from[l];
     for (int f : {2, 8, 16, kNoFlat}) {
@@ -1805,7 +1814,7 @@ puck_status puck_parser_autotune(puck_parser* P, const int32_t* word_ids, const 
 
 puck_status puck_parser_set_flat_from(puck_parser* p, int32_t level, int32_t span) {
   if (!p || level < 0 || level >= (int)p->levels.size() || span < 0 || span == 1 ||
-      (span > 0 && !p->levels[level]->flat_ready)) {
+      (span > 0 && !p->levels[level]->flat_ready_in && !p->levels[level]->flat_ready_out)) {
     set_error("puck_parser_set_flat_from: bad level or span, or a level without the flat-tile layout");
     return PUCK_ERR_INVALID_ARG;
   }
@@ -1815,7 +1824,8 @@ puck_status puck_parser_set_flat_from(puck_parser* p, int32_t level, int32_t spa
 
 int32_t puck_parser_flat_from(const puck_parser* p, int32_t level) {
   if (!p || level < 0 || level >= (int)p->levels.size()) return -1;
-  return p->levels[level]->flat_ready && p->flat_from[level] < kNoFlat ? p->flat_from[level] : 0;
+  const LevelDev& L = *p->levels[level];
+  return (L.flat_ready_in || L.flat_ready_out) && p->flat_from[level] < kNoFlat ? p->flat_from[level] : 0;
 }
 
 int32_t puck_parser_tensor_cores(const puck_parser* p, int32_t level, char* why, size_t len) {
