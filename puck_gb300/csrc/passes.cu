@@ -81,6 +81,8 @@ struct Smem {
   unsigned* pl;
   int* list;
   unsigned char* slist;  // per warp kSplitList: the live splits of the warp's current pair (flat-tile path)
+  float* sclist;         // sum-product levels, per warp kSplitList: the scale of each listed split, 0 for
+                         // the list's repeats (16-byte aligned)
   int mtile;             // floats of each warp's M tile
 };
 
@@ -106,6 +108,7 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
   m.pl = nullptr;
   m.list = nullptr;
   m.slist = nullptr;
+  m.sclist = nullptr;
   m.mtile = mtile_floats(L, flat);
   if (pairs) {
     if (with_stage) {
@@ -115,7 +118,13 @@ __device__ __forceinline__ Smem carve(float* base, const DevLevel& L, int chunk,
     m.M = rest;
     m.pl = reinterpret_cast<unsigned*>(rest + (blockDim.x >> 5) * m.mtile);
     m.list = reinterpret_cast<int*>(m.pl + L.n_coarse * L.mask_size);
-    if (with_stage) m.slist = reinterpret_cast<unsigned char*>(m.list + L.max_npair);
+    if (with_stage) {
+      m.slist = reinterpret_cast<unsigned char*>(m.list + L.max_npair);
+      if (L.semiring == SEMI_REAL) {
+        const size_t end = reinterpret_cast<size_t>(m.slist + (blockDim.x >> 5) * kSplitList);
+        m.sclist = reinterpret_cast<float*>((end + 15) & ~(size_t)15);
+      }
+    }
   } else {
     m.stA = rest;
     m.stB = rest + chunk * cs;
@@ -259,26 +268,25 @@ __device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned lon
 // This lane's operand value for each of the four splits of group g (see
 // grid_outer): one 4-byte load fetches the group's split positions from the
 // warp's live-split list, then their row pointers.
-// Sum-product: the positions past the pair's n live splits (the list's
-// repeats) add nothing, and the left operand (scl != nullptr) carries each
-// split's scale.
+// Sum-product: the left operand (sc != nullptr, the warp's scale list)
+// carries each listed split's scale, and the list's repeats have scale 0, so
+// they add nothing.
 template <int S>
-__device__ __forceinline__ float4 load_group(const float* const* rows, const float* scl, const unsigned char* sl,
-                                             int g, unsigned src, bool ok, int n) {
+__device__ __forceinline__ float4 load_group(const float* const* rows, const float* sc, const unsigned char* sl,
+                                             int g, unsigned src, bool ok) {
   const unsigned q = *reinterpret_cast<const unsigned*>(sl + 4 * g);
-  const unsigned i0 = q & 255u, i1 = (q >> 8) & 255u, i2 = (q >> 16) & 255u, i3 = q >> 24;
+  const float z = Sr<S>::zero();
   float4 v;
-  if (S == SEMI_VITERBI) {
-    v.x = ok ? __ldg(rows[i0] + src) : -CUDART_INF_F;
-    v.y = ok ? __ldg(rows[i1] + src) : -CUDART_INF_F;
-    v.z = ok ? __ldg(rows[i2] + src) : -CUDART_INF_F;
-    v.w = ok ? __ldg(rows[i3] + src) : -CUDART_INF_F;
-  } else {
-    const int b = 4 * g;
-    v.x = ok && b < n ? __ldg(rows[i0] + src) * (scl ? scl[i0] : 1.f) : 0.f;
-    v.y = ok && b + 1 < n ? __ldg(rows[i1] + src) * (scl ? scl[i1] : 1.f) : 0.f;
-    v.z = ok && b + 2 < n ? __ldg(rows[i2] + src) * (scl ? scl[i2] : 1.f) : 0.f;
-    v.w = ok && b + 3 < n ? __ldg(rows[i3] + src) * (scl ? scl[i3] : 1.f) : 0.f;
+  v.x = ok ? __ldg(rows[q & 255u] + src) : z;
+  v.y = ok ? __ldg(rows[(q >> 8) & 255u] + src) : z;
+  v.z = ok ? __ldg(rows[(q >> 16) & 255u] + src) : z;
+  v.w = ok ? __ldg(rows[q >> 24] + src) : z;
+  if (S == SEMI_REAL && sc) {
+    const float4 f = *reinterpret_cast<const float4*>(sc + 4 * g);
+    v.x *= f.x;
+    v.y *= f.y;
+    v.z *= f.z;
+    v.w *= f.w;
   }
   return v;
 }
@@ -300,8 +308,8 @@ __device__ __forceinline__ float4 load_group(const float* const* rows, const flo
 // B_s[Z_k], four fused multiply-adds per entry and group, the scale applied
 // to A when it is staged.
 template <int S, int RJ, int RK>
-__device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsigned char* sl, int n, int4 D,
-                                           float4* st4, float* Mw) {
+__device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsigned char* sl, const float* scl_list,
+                                           int n, int4 D, float4* st4, float* Mw) {
   const int lane = threadIdx.x & 31;
   const int ny = D.z & 255, nz = (D.z >> 8) & 255;
   const int jg = lane >> 2, kg = lane & 3;
@@ -320,10 +328,10 @@ __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsig
   const bool ok = mem < (a_side ? ny : nz);
   const unsigned src = (a_side ? (unsigned)D.x & 0xffffu : (unsigned)D.x >> 16) + mem;
   const float* const* rows = (a_side ? X.aptr : X.bptr) + c0;
-  const float* scl = S == SEMI_REAL && a_side ? X.scl + c0 : nullptr;
+  const float* sc = S == SEMI_REAL && a_side ? scl_list : nullptr;
   const int my_row = a_side ? mem : kStageRowB + mem;
   int g = 0;
-  float4 v = load_group<S>(rows, scl, sl, 0, src, ok, n);
+  float4 v = load_group<S>(rows, sc, sl, 0, src, ok);
   for (int buf = 0;; buf ^= 1) {
     float4* sb = st4 + buf * kStageRows;
     sb[my_row] = v;
@@ -331,7 +339,7 @@ __device__ __forceinline__ void grid_outer(const CellCtx& X, int c0, const unsig
     const bool rest = 4 * (g + 1) < n;
     if (rest) {
       ++g;
-      v = load_group<S>(rows, scl, sl, g, src, ok, n);
+      v = load_group<S>(rows, sc, sl, g, src, ok);
     }
     const char* stb = reinterpret_cast<const char*>(sb);
     float4 A[RJ];
@@ -415,6 +423,7 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   float4* st4 = reinterpret_cast<float4*>(sm.stage + warp * kStageFloats);
   unsigned char* sl = sm.slist + warp * kSplitList;
+  float* sc = S == SEMI_REAL ? sm.sclist + warp * kSplitList : nullptr;
   for (;;) {
     int k = 0;
     if (lane == 0) k = atomicAdd(&X.next, 1);
@@ -429,21 +438,33 @@ __device__ __forceinline__ void flat_pairs(const DevJob& J, const Smem& sm, Cell
         kFull, lane + 32 < nc && key_live(X.la[lane + 32], ca, grp) && key_live(X.lb[lane + 32], cb, grp));
     const unsigned long long m = (unsigned long long)lo | ((unsigned long long)hi << 32);
     // the pair's live splits in order, then three repeats of the last one
+    // (sum-product: with their scales, and scale 0 for the repeats)
     const unsigned below = (1u << lane) - 1u;
     const int nlo = __popc(lo), n = nlo + __popc(hi);
-    if ((lo >> lane) & 1u) sl[__popc(lo & below)] = (unsigned char)lane;
-    if ((hi >> lane) & 1u) sl[nlo + __popc(hi & below)] = (unsigned char)(32 + lane);
-    if (lane < 3) sl[n + lane] = (unsigned char)(hi ? 63 - __clz(hi) : 31 - __clz(lo));
+    if ((lo >> lane) & 1u) {
+      const int at = __popc(lo & below);
+      sl[at] = (unsigned char)lane;
+      if (S == SEMI_REAL) sc[at] = X.scl[c0 + lane];
+    }
+    if ((hi >> lane) & 1u) {
+      const int at = nlo + __popc(hi & below);
+      sl[at] = (unsigned char)(32 + lane);
+      if (S == SEMI_REAL) sc[at] = X.scl[c0 + 32 + lane];
+    }
+    if (lane < 3) {
+      sl[n + lane] = (unsigned char)(hi ? 63 - __clz(hi) : 31 - __clz(lo));
+      if (S == SEMI_REAL) sc[n + lane] = 0.f;
+    }
     __syncwarp();
     const int ny = D.z & 255, nz = (D.z >> 8) & 255, E = ny * nz;
     const int shape = (ny > 8 ? 3 : 0) + (nz > 12 ? 2 : nz > 8 ? 1 : 0);  // RJ in {1, 2} x RK in {2, 3, 4}
     switch (shape) {
-      case 0: grid_outer<S, 1, 2>(X, c0, sl, n, D, st4, Mw); break;
-      case 1: grid_outer<S, 1, 3>(X, c0, sl, n, D, st4, Mw); break;
-      case 2: grid_outer<S, 1, 4>(X, c0, sl, n, D, st4, Mw); break;
-      case 3: grid_outer<S, 2, 2>(X, c0, sl, n, D, st4, Mw); break;
-      case 4: grid_outer<S, 2, 3>(X, c0, sl, n, D, st4, Mw); break;
-      default: grid_outer<S, 2, 4>(X, c0, sl, n, D, st4, Mw); break;
+      case 0: grid_outer<S, 1, 2>(X, c0, sl, sc, n, D, st4, Mw); break;
+      case 1: grid_outer<S, 1, 3>(X, c0, sl, sc, n, D, st4, Mw); break;
+      case 2: grid_outer<S, 1, 4>(X, c0, sl, sc, n, D, st4, Mw); break;
+      case 3: grid_outer<S, 2, 2>(X, c0, sl, sc, n, D, st4, Mw); break;
+      case 4: grid_outer<S, 2, 3>(X, c0, sl, sc, n, D, st4, Mw); break;
+      default: grid_outer<S, 2, 4>(X, c0, sl, sc, n, D, st4, Mw); break;
     }
     if (lane == 0) work += (unsigned long long)__popcll(m) * E;
     flat_rules<S>(J, X, D, Mw, P, work, corner);
@@ -898,11 +919,11 @@ __device__ __forceinline__ void flush_counters(CellCtx& X, const Counters& C) {
 // Inside pass over the cells of a work list (span 1: the unary layer over
 // lexicon cells).  Register budgets: five CTAs per SM for the pair-factored
 // passes (48 registers: the flat-tile path keeps up to eight tile entries
-// and their stage offsets in registers), four for the sum-product flat-tile
-// pass (its staged loads also carry each split's scale: 80 spilled bytes at
-// 48 registers, none at 64), six for the target-major ones.
+// and their stage offsets in registers; the sum-product one spills 32 bytes
+// there and is still 18% faster than four CTAs at 63 registers), six for the
+// target-major ones.
 template <int S, int MODE>
-__global__ void __launch_bounds__(256, MODE == 3 && S == SEMI_REAL ? 4 : MODE >= 2 ? 5 : 6)
+__global__ void __launch_bounds__(256, MODE >= 2 ? 5 : 6)
     k_inside_span(DevLevel L, DevBatch B, DevWork W, DevMask M, float* inside, DevLive V, Counters C, int chunk) {
   extern __shared__ __align__(16) float smem[];
   __shared__ CellCtx X;
@@ -1232,7 +1253,8 @@ size_t pass_smem_bytes(const DevLevel& L, int chunk, bool with_stage, bool pairs
     return (2 * cs + (size_t)(kThreads / 32) * ((with_stage ? kStageFloats : 0) + mtile_floats(L, flat))) *
                sizeof(float) +
            (size_t)L.n_coarse * L.mask_size * sizeof(unsigned) + (size_t)L.max_npair * sizeof(int) +
-           (with_stage ? (size_t)(kThreads / 32) * kSplitList : 0);
+           (with_stage ? (size_t)(kThreads / 32) * kSplitList : 0) +
+           (with_stage && L.semiring == SEMI_REAL ? (size_t)(kThreads / 32) * kSplitList * sizeof(float) + 16 : 0);
   return (2 * cs + 2 * (size_t)chunk * cs) * sizeof(float);
 }
 
