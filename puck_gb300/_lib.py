@@ -52,7 +52,7 @@ class ServerStats(ctypes.Structure):
 
 EXPORTS = ("puck_default_options", "puck_default_compile_options", "puck_compile_grammar", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
            "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
-           "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells",
+           "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells", "puck_debug_flat_check",
            "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_parser_flat_from", "puck_parser_set_flat_from", "puck_parser_tensor_cores", "puck_mbr_decode_static",
            "puck_tc_selftest", "puck_server_create",
            "puck_server_destroy", "puck_server_now_ns", "puck_server_submit", "puck_server_poll",
@@ -105,6 +105,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_parser_autotune.restype = I
         L.puck_parser_tensor_cores.argtypes = [P, I, ctypes.c_char_p, ctypes.c_size_t]
         L.puck_parser_tensor_cores.restype = I
+        L.puck_debug_flat_check.argtypes = [P, I, I, I, ctypes.POINTER(ctypes.c_int64)]
+        L.puck_debug_flat_check.restype = I
         L.puck_parser_flat_from.argtypes = [P, I]
         L.puck_parser_flat_from.restype = I
         L.puck_parser_set_flat_from.argtypes = [P, I, I]

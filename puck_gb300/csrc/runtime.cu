@@ -311,9 +311,17 @@ const T* up(LevelDev& D, const HostLevel& L, const std::string& name, const char
 // nothing, when the job does not qualify.
 // ao/am and bo/bm: CSR from pair key to the operands' members (in the
 // operand roles' index spaces) for the left and right operands.
-bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const int* pk, const int* pbk,
-                      const int* bs, const int* bp, const int* pr, const float* pw, const int* seg_bits, int nseg,
-                      int ms, const int* ao, const int* am, const int* bo, const int* bm, float pad_w, int* mtile) {
+struct FlatHost {
+  std::vector<int4> desc, blk;
+  std::vector<int> key, gate, tgt;
+  std::vector<unsigned> idx;
+  std::vector<float4> w;
+  int max_tile = 1;
+};
+
+bool flat_tiles_host(FlatHost& F, int ntgt, int64_t npk, const int* pk, const int* pbk, const int* bs, const int* bp,
+                     const int* pr, const float* pw, const int* seg_bits, int nseg, int ms, const int* ao,
+                     const int* am, const int* bo, const int* bm, float pad_w) {
   constexpr int kSub = 16;  // largest sub-tile side
   auto contiguous = [](const int* off, const int* mem, int c) {
     for (int i = off[c]; i < off[c + 1]; ++i)
@@ -324,11 +332,14 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
     int t, e;
     float w;
   };
-  std::vector<int4> desc, blk;
-  std::vector<int> key, gate, tgt;
-  std::vector<unsigned> idx;
-  std::vector<float4> w;
-  int max_tile = 1;
+  std::vector<int4>& desc = F.desc;
+  std::vector<int4>& blk = F.blk;
+  std::vector<int>& key = F.key;
+  std::vector<int>& gate = F.gate;
+  std::vector<int>& tgt = F.tgt;
+  std::vector<unsigned>& idx = F.idx;
+  std::vector<float4>& w = F.w;
+  int& max_tile = F.max_tile;
   // One block of a sub-tile: rules sorted by target, at most 32 targets.
   auto emit_block = [&](int seg, const std::vector<FlatRule>& rs, int tile) -> bool {
     const int cnt = (int)rs.size();
@@ -474,7 +485,18 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
         max_tile = std::max(max_tile, sy * sz);
       }
   }
-  if (desc.size() > (size_t)INT32_MAX / 32) return false;
+  return desc.size() <= (size_t)INT32_MAX / 32;
+}
+
+// Uploads the flat-tile tables of a job (DevJob::flat).
+void upload_flat(LevelDev& D, puck::DevJob& J, FlatHost& F, int ms, float pad_w, int* mtile) {
+  std::vector<int4>& desc = F.desc;
+  std::vector<int4>& blk = F.blk;
+  std::vector<int>& key = F.key;
+  std::vector<int>& gate = F.gate;
+  std::vector<int>& tgt = F.tgt;
+  std::vector<unsigned>& idx = F.idx;
+  std::vector<float4>& w = F.w;
   J.fnpair = (int)desc.size();
   if (desc.empty()) desc.push_back(make_int4(0, 0, 0, 0));  // a job without rules still gets (never read) tables
   if (key.empty()) key.push_back(0);
@@ -493,7 +515,15 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
   J.fr_tgt = static_cast<const int*>(D.upload(tgt.data(), tgt.size() * sizeof(int)));
   J.fr_idx = static_cast<const unsigned*>(D.upload(idx.data(), idx.size() * sizeof(unsigned)));
   J.fr_w = static_cast<const float4*>(D.upload(w.data(), w.size() * sizeof(float4)));
-  *mtile = std::max(*mtile, max_tile);
+  *mtile = std::max(*mtile, F.max_tile);
+}
+
+bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const int* pk, const int* pbk,
+                      const int* bs, const int* bp, const int* pr, const float* pw, const int* seg_bits, int nseg,
+                      int ms, const int* ao, const int* am, const int* bo, const int* bm, float pad_w, int* mtile) {
+  FlatHost F;
+  if (!flat_tiles_host(F, ntgt, npk, pk, pbk, bs, bp, pr, pw, seg_bits, nseg, ms, ao, am, bo, bm, pad_w)) return false;
+  upload_flat(D, J, F, ms, pad_w, mtile);
   return true;
 }
 
@@ -505,7 +535,7 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
 // job's target-major table, grouped by (group of a, group of b), then by
 // segment and target.  Returns false, uploading nothing, when the level's
 // coarse maps do not rise strictly.
-bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int* mtile) {
+bool group_tiles_host(FlatHost& F, const HostLevel& L, int j, int nseg) {
   static const bool a_t[4] = {false, false, true, true};
   static const bool b_t[4] = {false, true, false, true};
   const std::string n = kJobNames[j];
@@ -575,9 +605,16 @@ bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, 
   }
   pbk.push_back((int)bs.size());
   bp.push_back((int)rs.size());
-  return build_flat_tiles(D, J, ntgt, (int64_t)pk.size(), pk.data(), pbk.data(), bs.data(), bp.data(), pr.data(),
-                          pw.data(), L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size, ao.data(),
-                          am.data(), bo.data(), bm.data(), -INFINITY, mtile);
+  return flat_tiles_host(F, ntgt, (int64_t)pk.size(), pk.data(), pbk.data(), bs.data(), bp.data(), pr.data(),
+                         pw.data(), L.get<int>(n + "/seg_bits", "i4", nullptr), nseg, L.mask_size, ao.data(),
+                         am.data(), bo.data(), bm.data(), -INFINITY);
+}
+
+bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int* mtile) {
+  FlatHost F;
+  if (!group_tiles_host(F, L, j, J.nseg)) return false;
+  upload_flat(D, J, F, L.mask_size, -INFINITY, mtile);
+  return true;
 }
 
 }  // namespace
@@ -1820,6 +1857,89 @@ puck_status puck_parser_set_flat_from(puck_parser* p, int32_t level, int32_t spa
   }
   p->flat_from[level] = span == 0 ? kNoFlat : span;
   return PUCK_OK;
+}
+
+int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job, int32_t groups, int64_t out[4]) {
+  try {
+    if (!g || level < 0 || level >= (int)g->levels.size() || job < 0 || job >= puck::NJOBS || (groups && job > 3))
+      return -3;
+    static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
+    static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
+    const HostLevel& L = g->levels[level];
+    const std::string n = kJobNames[job];
+    const float pad_w = L.semiring == puck::SEMI_REAL ? 0.f : -INFINITY;
+    int64_t nseg = 0;
+    L.get<int>(n + "/seg_bits", "i4", &nseg);
+    nseg /= std::max(1, L.mask_size);
+    int64_t nrow = 0;
+    const int* rowptr = L.get<int>(n + "/rowptr", "i4", &nrow);
+    const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
+    const float* wr = L.get<float>(n + "/w", "f4", nullptr);
+    FlatHost F;
+    bool ok;
+    if (groups) {
+      ok = group_tiles_host(F, L, job, (int)nseg);
+    } else {
+      int64_t npk = 0;
+      const int* pk = L.get<int>(n + "/pair_key", "i4", &npk);
+      ok = flat_tiles_host(F, (int)(nrow - 1), npk, pk, L.get<int>(n + "/pair_blk", "i4", nullptr),
+                           L.get<int>(n + "/blk_seg", "i4", nullptr), L.get<int>(n + "/blk_ptr", "i4", nullptr),
+                           L.get<int>(n + "/pair_rule", "i4", nullptr), L.get<float>(n + "/pair_w", "f4", nullptr),
+                           L.get<int>(n + "/seg_bits", "i4", nullptr), (int)nseg, L.mask_size,
+                           L.get<int>(a_t[job] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
+                           L.get<int>(a_t[job] ? "t_mem" : "nt_mem", "i4", nullptr),
+                           L.get<int>(b_t[job] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
+                           L.get<int>(b_t[job] ? "t_mem" : "nt_mem", "i4", nullptr), pad_w);
+    }
+    if (!ok) return -1;
+    // every rule the tables hold, as (target, a, b, weight bits) ...
+    using R = std::array<int64_t, 4>;
+    std::vector<R> got, want;
+    int64_t records = 0;
+    for (const int4& D : F.desc) {
+      const int a_first = D.x & 0xffff, b_first = (int)((unsigned)D.x >> 16);
+      const int sy = D.z & 255, sz = (D.z >> 8) & 255, nb = (int)((unsigned)D.z >> 16);
+      for (int q = D.y; q < D.y + nb; ++q) {
+        const int4 B = F.blk[q];
+        std::vector<int> tg;
+        for (int g0 = B.y; g0 < B.z; ++g0) {
+          ++records;
+          const int lane = (g0 - B.y) % 32, t = F.tgt[(size_t)q * 32 + lane];
+          for (int c = 0; c < 4; ++c) {
+            const float wt = (&F.w[g0].x)[c];
+            if (wt == pad_w || (std::isinf(pad_w) && std::isinf(wt) && wt < 0)) continue;
+            const int e = (int)((F.idx[g0] >> (8 * c)) & 255u);
+            if (t < 0 || e >= sy * sz) return -2;
+            uint32_t bits;
+            std::memcpy(&bits, &wt, 4);
+            got.push_back(R{t, a_first + e / sz, b_first + e % sz, bits});
+            tg.push_back(t);
+          }
+        }
+        std::sort(tg.begin(), tg.end());
+        if (std::unique(tg.begin(), tg.end()) - tg.begin() > 32) return -2;
+      }
+    }
+    // ... against the job's target-major rule table
+    for (int t = 0; t + 1 < nrow; ++t)
+      for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) {
+        uint32_t bits;
+        std::memcpy(&bits, &wr[r], 4);
+        want.push_back(R{t, ab[r] & 0xffff, (int64_t)((unsigned)ab[r] >> 16), bits});
+      }
+    std::sort(got.begin(), got.end());
+    std::sort(want.begin(), want.end());
+    if (out) {
+      out[0] = (int64_t)got.size();
+      out[1] = (int64_t)F.desc.size();
+      out[2] = (int64_t)F.blk.size();
+      out[3] = records;
+    }
+    return got == want ? 0 : -2;
+  } catch (const PuckError& e) {
+    set_error(e.msg);
+    return -3;
+  }
 }
 
 int32_t puck_parser_flat_from(const puck_parser* p, int32_t level) {

@@ -1,0 +1,75 @@
+"""Host-side check of the flat-tile tables (no GPU).
+
+The library builds, per job, sub-tiles of at most 16 x 16 members, blocks
+of at most 32 targets and bank-scheduled four-rule records; on the coarse
+level it builds the same layout over groups of 16 coarse ids.
+puck_debug_flat_check builds them as a parser would and rebuilds every rule
+they hold: the rules must equal the job's target-major rule table exactly
+(target, operands and weight bits), with every tile entry inside its tile.
+"""
+import ctypes
+
+import pytest
+
+from helpers import split_levels, write_grz
+from puck_gb300 import _lib
+
+JOBS = range(12)  # in_NN .. in_TT, then the eight outside jobs
+
+
+def _grammar(levels, name):
+    L = _lib.load()
+    st = ctypes.c_int32(0)
+    g = L.puck_grammar_load(write_grz(levels, name).encode(), ctypes.byref(st))
+    assert g, _lib.last_error()
+    return L, g
+
+
+@pytest.mark.parametrize("size,semiring", [("big", "viterbi"), ("deep", "viterbi"), ("wide", "viterbi"),
+                                           ("medium", "real"), ("big", "real")])
+def test_fine_level_flat_tables_hold_every_rule_once(size, semiring):
+    """25-33 refinements (sub-tiles of 16 + 16 + rest, blocks cut into runs
+    of 32 targets), up to 17, and many small pairs; Viterbi (padding -inf)
+    and sum-product (padding 0) weights; inside and outside jobs."""
+    levels = split_levels(semiring, size)
+    L, g = _grammar(levels, f"split_{size}" + ("_real" if semiring == "real" else ""))
+    try:
+        out = (ctypes.c_int64 * 4)()
+        subtiles = 0
+        for job in JOBS:
+            rc = L.puck_debug_flat_check(g, 1, job, 0, out)
+            assert rc == 0, (job, rc)
+            subtiles += out[1]
+        if size == "big":
+            assert subtiles > sum(len(levels[1].jobs[n]["pair_key"]) for n in levels[1].jobs
+                                  if "pair_key" in levels[1].jobs[n])  # pairs were cut
+    finally:
+        L.puck_grammar_free(g)
+
+
+@pytest.mark.parametrize("size", ["medium", "big"])
+def test_coarse_level_group_tables_hold_every_rule_once(size):
+    """The coarse level (one symbol per coarse id) as pairs of groups of 16
+    coarse ids, inside jobs."""
+    levels = split_levels("viterbi", size)
+    L, g = _grammar(levels, f"split_{size}")
+    try:
+        out = (ctypes.c_int64 * 4)()
+        for job in range(4):
+            rc = L.puck_debug_flat_check(g, 0, job, 1, out)
+            assert rc == 0, (job, rc)
+            assert out[0] == levels[0].jobs[["in_NN", "in_NT", "in_TN", "in_TT"][job]]["tgt"].shape[0]
+    finally:
+        L.puck_grammar_free(g)
+
+
+def test_flat_check_rejects_bad_arguments():
+    levels = split_levels("viterbi", "small")
+    L, g = _grammar(levels, "split_small")
+    try:
+        out = (ctypes.c_int64 * 4)()
+        assert L.puck_debug_flat_check(g, 2, 0, 0, out) == -3   # no such level
+        assert L.puck_debug_flat_check(g, 1, 12, 0, out) == -3  # no such job
+        assert L.puck_debug_flat_check(g, 0, 5, 1, out) == -3   # groups: inside jobs only
+    finally:
+        L.puck_grammar_free(g)
