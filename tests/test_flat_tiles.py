@@ -47,6 +47,24 @@ def test_fine_level_flat_tables_hold_every_rule_once(size, semiring):
         L.puck_grammar_free(g)
 
 
+def test_bench_grammar_flat_tables_hold_every_rule_once():
+    """The 1,091-symbol, 1.5M-rule bench grammar: all twelve jobs of its
+    fine level."""
+    levels = split_levels("viterbi", "c1")
+    L, g = _grammar(levels, "split_c1")
+    try:
+        out = (ctypes.c_int64 * 4)()
+        rules = 0
+        for job in range(4):
+            assert L.puck_debug_flat_check(g, 1, job, 0, out) == 0, job
+            rules += out[0]
+        assert rules == sum(levels[1].bucket_rules[b].shape[0] for b in range(4))
+        for job in range(4, 12):
+            assert L.puck_debug_flat_check(g, 1, job, 0, out) == 0, job
+    finally:
+        L.puck_grammar_free(g)
+
+
 @pytest.mark.parametrize("size", ["medium", "big"])
 def test_coarse_level_group_tables_hold_every_rule_once(size):
     """The coarse level (one symbol per coarse id) as pairs of groups of 16
