@@ -20,6 +20,13 @@
 // memory and several CTAs share an SM.  Grammars without split structure keep
 // target-major rule scans over operand cells staged in shared memory.
 //
+// Kernel modes: 0 target-major scans; 2 the pair form (whole-pair tiles, one
+// task of one j and four k per lane); 3 the flat-tile form (pairs cut into
+// 16 x 16 sub-tiles, an 8 x 4 lane grid over each, four-split groups staged
+// per warp, four-rule records), for both the max-plus and the sum-product
+// semiring and for both passes.  The host picks the mode per level and per
+// span launch.
+//
 // Reference semantics restated (dlwh/puck paths):
 //   gating        CLParser.scala:845-855,885-901 (segment bits vs cell mask, child "any")
 //   inside pass   CLParser.scala:256-314,489-504
@@ -37,7 +44,7 @@ using namespace dev;
 constexpr int kPairChunk = 64;   // splits per liveness chunk (two ballots)
 constexpr int kThreads = 256;
 constexpr int kRuleBatch = 4;   // rules per lane whose loads are in flight together
-// Per-warp operand stage of the Viterbi inside pass: two buffers of 34 rows
+// Per-warp operand stage of the flat-tile kernels: two buffers of 34 rows
 // of four floats (A members 0-15, a -inf row, B members 0-15, a -inf row).
 constexpr int kStageRows = 34;
 constexpr int kStageFloats = 2 * kStageRows * 4;
