@@ -411,6 +411,10 @@ def run_ours(args):
                      "avg_launch_ms": round(avg_launch_s * 1e3, 4)},
         "passes_ms_last_step": {
             f"level{l}": [round(v, 2) for v in P.pass_ms(l)[0]] for l in range(len(levels))},
+        # chart cells of a step (bot and top halves) and those whose coarse
+        # mask closes every fine symbol
+        "pruning": {"cells": int(s["cells"]), "cells_pruned": int(s["cells_pruned"]),
+                    "fraction": round(s["cells_pruned"] / max(s["cells"], 1), 4)},
     }
     P.release()
     if rank == 0 and world == 1:
@@ -673,7 +677,7 @@ def main():
                          "small: the plain method on the small PCFG")
     ap.add_argument("--fp64-subset", type=int, default=500)
     ap.add_argument("--tune-sample", type=int, default=2000, help="sentences the autotuner parses (0: no tuning)")
-    ap.add_argument("--long-sentences", type=int, default=1000)
+    ap.add_argument("--long-sentences", type=int, default=5000)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
