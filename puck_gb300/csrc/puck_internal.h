@@ -36,7 +36,7 @@ struct DevJob {
   // with j, k the operands' positions among their coarse symbol's members.
   int npair;
   int a_is_t, b_is_t;
-  int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs):
+  int interleaved;        // pair_rules lane-interleaved, tile-index form (Viterbi inside jobs, pair form):
                           // 1 mixed-target slices, 2 one target per lane slice (slice length a
                           // multiple of 4)
   const int* pair_key;    // [npair] ca | cb << 8
@@ -87,8 +87,8 @@ struct DevLevel {
   int flat_inside;  // every inside job with rules has the flat-tile layout (DevJob::flat); the
                     // host clears it in its copy of a level for launches of the other form
   int flat_outside; // the same for the outside jobs
-  int flat_mtile;   // largest ny * nz of any flat-tile sub-tile (<= 256); the M tile of the
-                    // Viterbi inside kernel when flat_inside
+  int flat_mtile;   // largest ny * nz of any flat-tile sub-tile (<= 256): the M tile of the
+                    // flat-tile (MODE 3) kernels
   int pair_group;   // coarse ids per pair key of the flat-tile tables: 1 (pairs of coarse
                     // symbols) or 16 (a target-major level whose coarse ids each have at
                     // most one member per role: pairs of groups of 16 coarse ids, liveness
