@@ -251,6 +251,58 @@ __device__ void gather_targets(const DevJob& J, const DevLevel& L, bool gated, f
   }
 }
 
+template <int S>
+__device__ __forceinline__ void flush_run(float* P, int t, float v, unsigned long long& corner);
+
+// Pair-major layout (DevJob::pm_*), for an ungated target-major level: every
+// thread takes distinct child pairs (a, b), computes max_s fl(A_s[a] +
+// B_s[b]) over the chunk's staged splits once (sum-product: the scaled sum),
+// and applies the pair's rules to their targets with shared-memory atomics.
+// Exact in max-plus: fl(max_s fl(A + B) + w) = max_s fl(fl(A + B) + w), as
+// for the pair-factored form.  The parts of a split cell take every G-th
+// pair.
+template <int S>
+__device__ void gather_pairmajor(const DevJob& J, const DevLevel& L, float* P, float* stA, float* stB, int chunk,
+                                 CellCtx& X) {
+  const int cs = L.cell_size;
+  const int lane = threadIdx.x & 31;
+  const int nsp = X.nsp;
+  unsigned long long work = 0, corner = 0;
+  for (int c0 = 0; c0 < nsp; c0 += chunk) {
+    const int nc = min(chunk, nsp - c0);
+    stage(X, c0, nc, cs, stA, stB);
+    __syncthreads();
+    for (int p = X.g * blockDim.x + threadIdx.x; p < J.pm_npair; p += X.G * blockDim.x) {
+      const int ab = __ldg(J.pm_ab + p);
+      const int a = ab & 0xffff, b = (int)((unsigned)ab >> 16);
+      float v = Sr<S>::zero();
+      if (S == SEMI_VITERBI) {
+        for (int s = 0; s < nc; ++s) v = fmaxf(v, stA[s * cs + a] + stB[s * cs + b]);
+      } else {
+        for (int s = 0; s < nc; ++s) v = fmaf(X.scl[c0 + s], stA[s * cs + a] * stB[s * cs + b], v);
+      }
+      const int r0 = __ldg(J.pm_off + p), r1 = __ldg(J.pm_off + p + 1);
+      work += (unsigned long long)nc + (r1 - r0);
+      if (v == Sr<S>::zero()) continue;
+      for (int r = r0; r < r1; ++r) {
+        const int2 R = __ldg(J.pm_rule + r);
+        const float w = __int_as_float(R.y);
+        flush_run<S>(P, R.x, S == SEMI_VITERBI ? v + w : v * w, corner);
+      }
+    }
+    __syncthreads();
+  }
+  if (nsp == 0) __syncthreads();  // see gather()
+  for (int o = 16; o > 0; o >>= 1) {
+    work += __shfl_down_sync(kFull, work, o);
+    corner += __shfl_down_sync(kFull, corner, o);
+  }
+  if (lane == 0 && (work | corner)) {
+    atomicAdd(&X.work, work);
+    atomicAdd(&X.corner, corner);
+  }
+}
+
 __device__ __forceinline__ bool bit(const int* words, int c) { return (words[c >> 5] >> (c & 31)) & 1; }
 
 // Whether pair key c has a live member in the liveness words: key = one
@@ -825,6 +877,7 @@ __device__ __forceinline__ void gather(const DevJob& J, const DevLevel& L, bool 
                                        int chunk, CellCtx& X) {
   if constexpr (MODE == 3) gather_pairs<S, true>(J, L, gated, P, sm, X);
   else if constexpr (MODE == 2 && S != SEMI_LOGSUM) gather_pairs<S>(J, L, gated, P, sm, X);
+  else if (S != SEMI_LOGSUM && !gated && J.pm_npair > 0) gather_pairmajor<S>(J, L, P, sm.stA, sm.stB, chunk, X);
   else gather_targets<S>(J, L, gated, P, sm.stA, sm.stB, chunk, X);
 }
 

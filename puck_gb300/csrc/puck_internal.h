@@ -69,6 +69,13 @@ struct DevJob {
   const int* fr_tgt;      // [nblk * 32] target of each lane's slice, -1 for none
   const unsigned* fr_idx; // [records] four tile entries, byte q = rule q
   const float4* fr_w;     // [records] four weights
+  // Pair-major layout (target-major levels, Viterbi and sum-product): the
+  // job's rules grouped by their distinct child pair (a, b), for the scan of
+  // an ungated level that computes each pair's split maximum (or sum) once.
+  int pm_npair;
+  const int* pm_ab;       // [pm_npair] a | b << 16
+  const int* pm_off;      // [pm_npair + 1] rule range of each pair
+  const int2* pm_rule;    // {target, bits(w)}
 };
 
 struct DevUJob {

@@ -829,6 +829,41 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
   d.flat_outside = 1;
   for (int j = 0; j < puck::NJOBS; ++j)
     if (d.jobs[j].nseg > 0 && d.jobs[j].n_tgt > 0 && !d.jobs[j].flat) (j <= puck::IN_TT ? d.flat_inside : d.flat_outside) = 0;
+  // Target-major levels also get each job's rules grouped by child pair (the
+  // pair-major scan of an ungated level).
+  if (L.semiring != puck::SEMI_LOGSUM && L.get<int>("in_NN/pair_mode", "i4", nullptr)[0] != 2) {
+    for (int j = 0; j < puck::NJOBS; ++j) {
+      puck::DevJob& J = d.jobs[j];
+      const std::string n = kJobNames[j];
+      int64_t nrow = 0;
+      const int* rowptr = L.get<int>(n + "/rowptr", "i4", &nrow);
+      const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
+      const float* w = L.get<float>(n + "/w", "f4", nullptr);
+      std::vector<std::array<int, 3>> rs;  // (a | b << 16, target, rule)
+      for (int t = 0; t + 1 < nrow; ++t)
+        for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) rs.push_back({ab[r], t, r});
+      std::sort(rs.begin(), rs.end());
+      std::vector<int> pab, poff;
+      std::vector<int2> prule;
+      for (size_t i = 0; i < rs.size(); ++i) {
+        if (i == 0 || rs[i][0] != rs[i - 1][0]) {
+          pab.push_back(rs[i][0]);
+          poff.push_back((int)prule.size());
+        }
+        int2 v;
+        v.x = rs[i][1];
+        std::memcpy(&v.y, &w[rs[i][2]], 4);
+        prule.push_back(v);
+      }
+      poff.push_back((int)prule.size());
+      J.pm_npair = (int)pab.size();
+      if (pab.empty()) pab.push_back(0);
+      if (prule.empty()) prule.push_back(make_int2(0, 0));
+      J.pm_ab = static_cast<const int*>(D.upload(pab.data(), pab.size() * sizeof(int)));
+      J.pm_off = static_cast<const int*>(D.upload(poff.data(), poff.size() * sizeof(int)));
+      J.pm_rule = static_cast<const int2*>(D.upload(prule.data(), prule.size() * sizeof(int2)));
+    }
+  }
   d.pair_group = 1;
   {
     const int* nn_mode = L.get<int>("in_NN/pair_mode", "i4", nullptr);
