@@ -155,15 +155,17 @@ puck_status puck_inside_outside(puck_parser* p, const int32_t* word_ids, const i
  * (num_cells floats), 5 per-cell MBR {score, symbol} pairs (num_cells * 2). */
 puck_status puck_debug_copy(puck_parser* p, int32_t level, int32_t which, void* host_out, size_t bytes);
 int64_t puck_debug_num_cells(const puck_parser* p);
-/* Host-only check of the flat-tile tables of one job (no device needed):
- * builds them as a parser would (groups != 0: over groups of 16 coarse ids,
- * inside jobs 0-3 only) and rebuilds every rule they hold, which must equal
- * the job's target-major rule table exactly (target, operands, weight bits).
- * out[0..3] = rules, sub-tiles, blocks, records.  Returns 0 when they match,
- * -1 when the job does not take the layout, -2 on a mismatch or a broken
- * invariant (an entry outside its tile, more than 32 targets in a block),
- * -3 for bad arguments. */
-int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job, int32_t groups, int64_t out[4]);
+/* Host-only check of a job's rule tables (no device needed): builds them as
+ * a parser would and rebuilds every rule they hold, which must equal the
+ * job's target-major rule table exactly (target, operands, weight bits).
+ * form: 0 the flat-tile tables over coarse pairs, 1 the flat-tile tables over
+ * groups of 16 coarse ids (inside jobs 0-3 only), 2 the pair-major tables.
+ * out[0..3] = rules, then sub-tiles, blocks, records (form 0-1) or distinct
+ * pairs (form 2).  Returns 0 when they match, -1 when the job does not take
+ * the layout, -2 on a mismatch or a broken invariant (an entry outside its
+ * tile, more than 32 targets in a block, a pair listed twice), -3 for bad
+ * arguments. */
+int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job, int32_t form, int64_t out[4]);
 
 puck_status puck_parser_stats(const puck_parser* p, puck_stats* out);
 

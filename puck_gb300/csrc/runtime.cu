@@ -617,6 +617,42 @@ bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, 
   return true;
 }
 
+// Pair-major tables of one job (DevJob::pm_*): the job's rules grouped by
+// their child pair (a, b), each pair's rules as {target, bits(w)}.  Returns
+// false for a job whose targets average more than kPairMajorRules rules
+// (the atomic updates of each target would serialise) or that has none.
+constexpr int kPairMajorRules = 48;
+bool pm_tables_host(const HostLevel& L, int j, std::vector<int>& pab, std::vector<int>& poff,
+                    std::vector<int2>& prule) {
+  const std::string n = kJobNames[j];
+  int64_t nrow = 0;
+  const int* rowptr = L.get<int>(n + "/rowptr", "i4", &nrow);
+  const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
+  const float* w = L.get<float>(n + "/w", "f4", nullptr);
+  int with_rules = 0;
+  for (int t = 0; t + 1 < nrow; ++t) with_rules += rowptr[t + 1] > rowptr[t];
+  if (with_rules == 0 || rowptr[nrow - 1] > (int64_t)kPairMajorRules * with_rules) return false;
+  std::vector<std::array<int, 3>> rs;  // (a | b << 16, target, rule)
+  for (int t = 0; t + 1 < nrow; ++t)
+    for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) rs.push_back({ab[r], t, r});
+  std::sort(rs.begin(), rs.end());
+  pab.clear();
+  poff.clear();
+  prule.clear();
+  for (size_t i = 0; i < rs.size(); ++i) {
+    if (i == 0 || rs[i][0] != rs[i - 1][0]) {
+      pab.push_back(rs[i][0]);
+      poff.push_back((int)prule.size());
+    }
+    int2 v;
+    v.x = rs[i][1];
+    std::memcpy(&v.y, &w[rs[i][2]], 4);
+    prule.push_back(v);
+  }
+  poff.push_back((int)prule.size());
+  return true;
+}
+
 }  // namespace
 
 void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
@@ -834,38 +870,13 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
   // most kPairMajorRules rules on average: with more, the atomic updates of
   // each target serialise (a 64 + 32-symbol grammar of 20,000 rules, 137 per
   // NN target, parsed 10% slower that way).
-  constexpr int kPairMajorRules = 48;
   if (L.semiring != puck::SEMI_LOGSUM && L.get<int>("in_NN/pair_mode", "i4", nullptr)[0] != 2) {
+    std::vector<int> pab, poff;
+    std::vector<int2> prule;
     for (int j = 0; j < puck::NJOBS; ++j) {
+      if (!pm_tables_host(L, j, pab, poff, prule)) continue;
       puck::DevJob& J = d.jobs[j];
-      const std::string n = kJobNames[j];
-      int64_t nrow = 0;
-      const int* rowptr = L.get<int>(n + "/rowptr", "i4", &nrow);
-      int with_rules = 0;
-      for (int t = 0; t + 1 < nrow; ++t) with_rules += rowptr[t + 1] > rowptr[t];
-      if (with_rules == 0 || rowptr[nrow - 1] > (int64_t)kPairMajorRules * with_rules) continue;
-      const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
-      const float* w = L.get<float>(n + "/w", "f4", nullptr);
-      std::vector<std::array<int, 3>> rs;  // (a | b << 16, target, rule)
-      for (int t = 0; t + 1 < nrow; ++t)
-        for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) rs.push_back({ab[r], t, r});
-      std::sort(rs.begin(), rs.end());
-      std::vector<int> pab, poff;
-      std::vector<int2> prule;
-      for (size_t i = 0; i < rs.size(); ++i) {
-        if (i == 0 || rs[i][0] != rs[i - 1][0]) {
-          pab.push_back(rs[i][0]);
-          poff.push_back((int)prule.size());
-        }
-        int2 v;
-        v.x = rs[i][1];
-        std::memcpy(&v.y, &w[rs[i][2]], 4);
-        prule.push_back(v);
-      }
-      poff.push_back((int)prule.size());
       J.pm_npair = (int)pab.size();
-      if (pab.empty()) pab.push_back(0);
-      if (prule.empty()) prule.push_back(make_int2(0, 0));
       J.pm_ab = static_cast<const int*>(D.upload(pab.data(), pab.size() * sizeof(int)));
       J.pm_off = static_cast<const int*>(D.upload(poff.data(), poff.size() * sizeof(int)));
       J.pm_rule = static_cast<const int2*>(D.upload(prule.data(), prule.size() * sizeof(int2)));
@@ -1901,9 +1912,10 @@ puck_status puck_parser_set_flat_from(puck_parser* p, int32_t level, int32_t spa
   return PUCK_OK;
 }
 
-int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job, int32_t groups, int64_t out[4]) {
+int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job, int32_t form, int64_t out[4]) {
   try {
-    if (!g || level < 0 || level >= (int)g->levels.size() || job < 0 || job >= puck::NJOBS || (groups && job > 3))
+    if (!g || level < 0 || level >= (int)g->levels.size() || job < 0 || job >= puck::NJOBS || form < 0 ||
+        form > 2 || (form == 1 && job > 3))
       return -3;
     static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
     static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
@@ -1917,9 +1929,35 @@ int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job,
     const int* rowptr = L.get<int>(n + "/rowptr", "i4", &nrow);
     const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
     const float* wr = L.get<float>(n + "/w", "f4", nullptr);
+    using R = std::array<int64_t, 4>;
+    std::vector<R> got, want;
+    for (int t = 0; t + 1 < nrow; ++t)
+      for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) {
+        uint32_t bits;
+        std::memcpy(&bits, &wr[r], 4);
+        want.push_back(R{t, ab[r] & 0xffff, (int64_t)((unsigned)ab[r] >> 16), bits});
+      }
+    std::sort(want.begin(), want.end());
+    if (form == 2) {  // the pair-major tables: every pair's rules, pairs distinct
+      std::vector<int> pab, poff;
+      std::vector<int2> prule;
+      if (!pm_tables_host(L, job, pab, poff, prule)) return -1;
+      for (size_t p = 0; p < pab.size(); ++p) {
+        if (p > 0 && pab[p] == pab[p - 1]) return -2;
+        for (int r = poff[p]; r < poff[p + 1]; ++r)
+          got.push_back(R{prule[r].x, pab[p] & 0xffff, (int64_t)((unsigned)pab[p] >> 16), (uint32_t)prule[r].y});
+      }
+      std::sort(got.begin(), got.end());
+      if (out) {
+        out[0] = (int64_t)got.size();
+        out[1] = (int64_t)pab.size();
+        out[2] = out[3] = 0;
+      }
+      return got == want ? 0 : -2;
+    }
     FlatHost F;
     bool ok;
-    if (groups) {
+    if (form == 1) {
       ok = group_tiles_host(F, L, job, (int)nseg);
     } else {
       int64_t npk = 0;
@@ -1934,9 +1972,8 @@ int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job,
                            L.get<int>(b_t[job] ? "t_mem" : "nt_mem", "i4", nullptr), pad_w);
     }
     if (!ok) return -1;
-    // every rule the tables hold, as (target, a, b, weight bits) ...
-    using R = std::array<int64_t, 4>;
-    std::vector<R> got, want;
+    // every rule the tables hold, as (target, a, b, weight bits), against the
+    // job's target-major rule table
     int64_t records = 0;
     for (const int4& D : F.desc) {
       const int a_first = D.x & 0xffff, b_first = (int)((unsigned)D.x >> 16);
@@ -1962,15 +1999,7 @@ int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job,
         if (std::unique(tg.begin(), tg.end()) - tg.begin() > 32) return -2;
       }
     }
-    // ... against the job's target-major rule table
-    for (int t = 0; t + 1 < nrow; ++t)
-      for (int r = rowptr[t]; r < rowptr[t + 1]; ++r) {
-        uint32_t bits;
-        std::memcpy(&bits, &wr[r], 4);
-        want.push_back(R{t, ab[r] & 0xffff, (int64_t)((unsigned)ab[r] >> 16), bits});
-      }
     std::sort(got.begin(), got.end());
-    std::sort(want.begin(), want.end());
     if (out) {
       out[0] = (int64_t)got.size();
       out[1] = (int64_t)F.desc.size();

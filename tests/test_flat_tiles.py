@@ -1,4 +1,4 @@
-"""Host-side check of the flat-tile tables (no GPU).
+"""Host-side check of the flat-tile and pair-major tables (no GPU).
 
 The library builds, per job, sub-tiles of at most 16 x 16 members, blocks
 of at most 32 targets and bank-scheduled four-rule records; on the coarse
@@ -11,7 +11,7 @@ import ctypes
 
 import pytest
 
-from helpers import split_levels, write_grz
+from helpers import small_pcfg_levels, split_levels, write_grz
 from puck_gb300 import _lib
 
 JOBS = range(12)  # in_NN .. in_TT, then the eight outside jobs
@@ -81,6 +81,34 @@ def test_coarse_level_group_tables_hold_every_rule_once(size):
         L.puck_grammar_free(g)
 
 
+@pytest.mark.parametrize("size", ["medium", "c1"])
+def test_coarse_level_pair_major_tables_hold_every_rule_once(size):
+    """The coarse level's pair-major tables (every job: each distinct child
+    pair once, with all of its rules)."""
+    levels = split_levels("viterbi", size)
+    L, g = _grammar(levels, f"split_{size}")
+    try:
+        out = (ctypes.c_int64 * 4)()
+        for job in JOBS:
+            assert L.puck_debug_flat_check(g, 0, job, 2, out) == 0, job
+            assert 0 < out[1] <= out[0]
+    finally:
+        L.puck_grammar_free(g)
+
+
+def test_pair_major_tables_skip_dense_targets():
+    """A job whose targets average more than 48 rules keeps the target-major
+    scan: the 64 + 32-symbol plain grammar's NN job (137 per target)."""
+    levels = small_pcfg_levels()
+    L, g = _grammar(levels, "small_pcfg")
+    try:
+        out = (ctypes.c_int64 * 4)()
+        assert L.puck_debug_flat_check(g, 0, 0, 2, out) == -1   # in_NN
+        assert L.puck_debug_flat_check(g, 0, 3, 2, out) == 0    # in_TT, 34 per target
+    finally:
+        L.puck_grammar_free(g)
+
+
 def test_flat_check_rejects_bad_arguments():
     levels = split_levels("viterbi", "small")
     L, g = _grammar(levels, "split_small")
@@ -89,5 +117,6 @@ def test_flat_check_rejects_bad_arguments():
         assert L.puck_debug_flat_check(g, 2, 0, 0, out) == -3   # no such level
         assert L.puck_debug_flat_check(g, 1, 12, 0, out) == -3  # no such job
         assert L.puck_debug_flat_check(g, 0, 5, 1, out) == -3   # groups: inside jobs only
+        assert L.puck_debug_flat_check(g, 0, 0, 3, out) == -3   # no such form
     finally:
         L.puck_grammar_free(g)
