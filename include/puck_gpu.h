@@ -105,6 +105,15 @@ int32_t puck_grammar_num_levels(const puck_grammar* g);
 puck_status puck_grammar_level_info(const puck_grammar* g, int32_t level, int32_t out[8]);
 /* Word string -> id in the vocabulary of the fine level; -1 if unknown. */
 int32_t puck_grammar_word_id(const puck_grammar* g, const char* word);
+/* The word's id, else the id of its unknown-word class for a word at
+ * `position` in its sentence (0 = first), backing off to ever shorter
+ * classes and finally "UNK", else -1.  The classes are those of the
+ * Berkeley parser's English lexicons, which list one entry per class
+ * (`UNK-INITC-KNOWNLC`, `UNK-LC-s`, ...): capitalisation (INITC with
+ * KNOWNLC, CAPS, LC), digits (NUM), hyphens (DASH) and an English suffix.
+ * The reference takes unknown-word scores from epic's lexicon model, which
+ * is not present here, so this mapping is not checked against it. */
+int32_t puck_grammar_word_id_at(const puck_grammar* g, const char* word, int32_t position);
 
 /* --- grammar compiler (CompileGrammar.main, CompileGrammar.scala:20-72) -- */
 /* Options of CompileGrammar (CompileGrammar.scala:20-25). */

@@ -51,7 +51,7 @@ class ServerStats(ctypes.Structure):
 
 
 EXPORTS = ("puck_default_options", "puck_default_compile_options", "puck_compile_grammar", "puck_grammar_load", "puck_grammar_free", "puck_grammar_num_levels",
-           "puck_grammar_level_info", "puck_grammar_word_id", "puck_parser_create", "puck_parser_destroy",
+           "puck_grammar_level_info", "puck_grammar_word_id", "puck_grammar_word_id_at", "puck_parser_create", "puck_parser_destroy",
            "puck_parse", "puck_partitions", "puck_inside_outside", "puck_debug_copy", "puck_debug_num_cells", "puck_debug_flat_check",
            "puck_parser_stats", "puck_parser_pass_ms", "puck_parser_level_work", "puck_parser_autotune", "puck_parser_flat_from", "puck_parser_set_flat_from", "puck_parser_tensor_cores", "puck_mbr_decode_static",
            "puck_tc_selftest", "puck_server_create",
@@ -82,6 +82,8 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_grammar_level_info.restype = I
         L.puck_grammar_word_id.argtypes = [P, ctypes.c_char_p]
         L.puck_grammar_word_id.restype = I
+        L.puck_grammar_word_id_at.argtypes = [P, ctypes.c_char_p, I]
+        L.puck_grammar_word_id_at.restype = I
         L.puck_parser_create.restype = P
         L.puck_parser_create.argtypes = [P, ctypes.POINTER(Options), ctypes.POINTER(I)]
         L.puck_parser_destroy.argtypes = [P]

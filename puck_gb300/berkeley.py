@@ -18,8 +18,12 @@ log score is below ``threshold`` (epic's -12) are dropped.  Every
 nonterminal substate gets an identity unary ``X_i -> X_i`` with score 0 when
 the file has none, because the unary layer replaces the whole top cell (the
 reference's unary bucket includes identities, RuleStructure.scala:86-97).
-Unknown words have no lexicon entries here (epic's signature model is out of
-scope); the parser reports them as out of vocabulary.
+The lexicon's unknown-word classes (``UNK-INITC-s``, ``UNK-LC``, ...) are
+ordinary words of the vocabulary.  The library maps a word missing from the
+vocabulary to its class by its spelling and position
+(``puck_grammar_word_id_at``); epic's own lexicon model, which the reference
+uses, is not present, so that mapping is not checked against it.  A word
+with no class in the lexicon is out of vocabulary.
 
 A cascade (``a:b``) shares one coarse label set (the union of the levels'
 numstates labels, first level first) and one vocabulary (the union of the

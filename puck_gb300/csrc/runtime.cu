@@ -617,6 +617,74 @@ bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, 
   return true;
 }
 
+// The unknown-word class of a word, in the scheme of the Berkeley parser's
+// English lexicons, whose text grammars list one lexicon entry per class
+// (`UNK-INITC-KNOWNLC`, `UNK-LC-s`, `UNK-CAPS-NUM`, ...):
+//   "UNK";
+//   a capitalisation class: -INITC for a sentence-initial word whose only
+//   capital is its first letter (plus -KNOWNLC when its lowercase form is a
+//   known word), -CAPS for any other word starting with a capital or for a
+//   word with a capital after a non-letter start, -LC for other words with a
+//   lowercase letter;
+//   -NUM when it has a digit, -DASH when it has a hyphen;
+//   one suffix class: -s for a final s after anything but s, i or u in a word
+//   of three or more characters; otherwise, for words of five or more
+//   characters without a hyphen and without both a digit and a capital, the
+//   first of -ed, -ing, -ion, -er, -est, -ly, -ity, -y, -al that ends the
+//   lowercased word.
+// Letters are ASCII; other bytes count as neither letters nor digits.
+std::string unknown_word_class(const std::string& w, int position,
+                               const std::unordered_map<std::string, int>& known) {
+  int caps = 0;
+  bool digit = false, dash = false, lower = false;
+  std::string lc(w);
+  for (char& c : lc) {
+    const unsigned char u = (unsigned char)c;
+    if (u >= '0' && u <= '9') digit = true;
+    else if (u == '-') dash = true;
+    else if (u >= 'a' && u <= 'z') lower = true;
+    else if (u >= 'A' && u <= 'Z') {
+      ++caps;
+      c = (char)(u - 'A' + 'a');
+    }
+  }
+  const unsigned char first = (unsigned char)w[0];
+  const bool first_cap = first >= 'A' && first <= 'Z';
+  const bool first_letter = first_cap || (first >= 'a' && first <= 'z');
+  std::string sig = "UNK";
+  if (first_cap) {
+    if (position == 0 && caps == 1) {
+      sig += "-INITC";
+      if (known.count(lc)) sig += "-KNOWNLC";
+    } else {
+      sig += "-CAPS";
+    }
+  } else if (!first_letter && caps > 0) {
+    sig += "-CAPS";
+  } else if (lower) {
+    sig += "-LC";
+  }
+  if (digit) sig += "-NUM";
+  if (dash) sig += "-DASH";
+  const size_t n = lc.size();
+  auto ends = [&](const char* suf) {
+    const size_t k = std::strlen(suf);
+    return n >= k && lc.compare(n - k, k, suf) == 0;
+  };
+  if (n >= 3 && lc[n - 1] == 's') {
+    const char before = lc[n - 2];
+    if (before != 's' && before != 'i' && before != 'u') sig += "-s";
+  } else if (n >= 5 && !dash && !(digit && caps > 0)) {
+    for (const char* suf : {"ed", "ing", "ion", "er", "est", "ly", "ity", "y", "al"})
+      if (ends(suf)) {
+        sig += "-";
+        sig += suf;
+        break;
+      }
+  }
+  return sig;
+}
+
 // Pair-major tables of one job (DevJob::pm_*): the job's rules grouped by
 // their child pair (a, b), each pair's rules as {target, bits(w)}.  Returns
 // false for a job whose targets average more than kPairMajorRules rules
@@ -1705,6 +1773,21 @@ int32_t puck_grammar_word_id(const puck_grammar* g, const char* word) {
   if (!g || !word) return -1;
   auto it = g->word_index.find(word);
   return it == g->word_index.end() ? -1 : it->second;
+}
+
+int32_t puck_grammar_word_id_at(const puck_grammar* g, const char* word, int32_t position) {
+  if (!g || !word || !*word) return -1;
+  auto it = g->word_index.find(word);
+  if (it != g->word_index.end()) return it->second;
+  // the unknown-word class, then ever shorter prefixes of it ("UNK" last)
+  std::string sig = unknown_word_class(word, position, g->word_index);
+  for (;;) {
+    auto s = g->word_index.find(sig);
+    if (s != g->word_index.end()) return s->second;
+    const size_t cut = sig.rfind('-');
+    if (cut == std::string::npos) return -1;
+    sig.resize(cut);
+  }
 }
 
 puck_parser* puck_parser_create(const puck_grammar* g, const puck_options* opts, puck_status* status) {

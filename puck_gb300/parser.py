@@ -217,12 +217,14 @@ class CLParser:
 
     # -- word handling ----------------------------------------------------
     def word_ids(self, sentence: Sequence[Union[str, int]]) -> List[int]:
+        # a word missing from the lexicon takes its unknown-word class where
+        # the lexicon has one (puck_grammar_word_id_at)
         out = []
-        for w in sentence:
+        for i, w in enumerate(sentence):
             if isinstance(w, (int, np.integer)):
                 out.append(int(w))
             else:
-                out.append(self._L.puck_grammar_word_id(self._g, str(w).encode()))
+                out.append(self._L.puck_grammar_word_id_at(self._g, str(w).encode(), i))
         return out
 
     @property
