@@ -16,12 +16,21 @@ It fills each cell straight from the rule lists of a compiled level:
 Viterbi charts must agree bit for bit (max is exact and each candidate is
 ``(left + right) + rule`` in float32, the order the device kernels use).
 Sum-product is checked through log Z against a float64 log-space CKY.
+
+The cascade is restated the same way: the coarse level's outside pass
+scattered from each parent cell to its children (the oracle gathers per
+child), the pruning masks from ``inside + outside >= root - 9``
+(CLParser.scala computeMasks), and the fine level's inside pass under those
+masks with the reference's gating: a rule runs at a parent cell when the
+cell's mask meets the coarse bits of the rule's segment
+(CoarseParentSymbolGrammarClusterer: one segment per large coarse parent,
+one for the rest), and a split only when both child cells hold a live bit.
 """
 import numpy as np
 import pytest
 
 import oracle
-from helpers import small_pcfg_levels, tiny_pcfg_levels
+from helpers import small_pcfg_levels, split_levels, split_sentences, tiny_pcfg_levels
 from puck_gb300 import grammar, synth
 
 NEG = np.float32(-np.inf)
@@ -32,12 +41,18 @@ def _chart_index(b, e, n):
     return b + sp * n - sp * (sp - 1) // 2
 
 
-def _viterbi_cky(cl, words):
+def _viterbi_cky(cl, words, mbot=None, mtop=None):
+    """Inside pass.  ``mbot``/``mtop`` (int32[n+1, n+1, mask_size]) are the
+    coarse level's masks; None runs unpruned."""
     n, cs = len(words), cl.cell_size
     bot = np.full((n + 1, n + 1, cs), NEG, np.float32)
     top = np.full((n + 1, n + 1, cs), NEG, np.float32)
     nu_p, nu_c = cl.nu_rules[:, 0], cl.nu_rules[:, 1]
     tu_p, tu_c = cl.tu_rules[:, 0], cl.tu_rules[:, 1]
+    names = {grammar.NN: "in_NN", grammar.NT: "in_NT", grammar.TN: "in_TN", grammar.TT: "in_TT"}
+
+    def live(m, b, e):
+        return m is None or bool(np.any(m[b, e]))
 
     def unary(dst, src, p, c, w):
         dst[:] = NEG
@@ -46,25 +61,101 @@ def _viterbi_cky(cl, words):
     for i, w in enumerate(words):
         lo, hi = cl.lex_offsets[w], cl.lex_offsets[w + 1]
         bot[i, i + 1, cl.lex_term[lo:hi]] = cl.lex_score[lo:hi]
-        unary(top[i, i + 1], bot[i, i + 1], tu_p, tu_c, cl.tu_scores)
+        if live(mtop, i, i + 1):
+            unary(top[i, i + 1], bot[i, i + 1], tu_p, tu_c, cl.tu_scores)
 
-    def binary(dst, left, right, bucket):
+    def binary(dst, left, right, bucket, b, e, lcell, rcell):
         r, w = cl.bucket_rules[bucket], cl.bucket_scores[bucket]
-        if r.shape[0]:
-            np.maximum.at(dst, r[:, 0], ((left[r[:, 1]] + right[r[:, 2]]) + w).astype(np.float32))
+        if not r.shape[0] or not (live(lcell[0], *lcell[1:]) and live(rcell[0], *rcell[1:])):
+            return
+        if mbot is not None:
+            job = cl.jobs[names[bucket]]
+            gate = job["seg_bits"][job["tgt_seg"][r[:, 0]]]
+            keep = np.any(gate & mbot[b, e], axis=1)
+            r, w = r[keep], w[keep]
+        np.maximum.at(dst, r[:, 0], ((left[r[:, 1]] + right[r[:, 2]]) + w).astype(np.float32))
 
     for span in range(2, n + 1):
         for b in range(n - span + 1):
             e = b + span
             cell = bot[b, e]
             if span == 2:
-                binary(cell, bot[b, b + 1], bot[b + 1, e], grammar.TT)
-            binary(cell, top[b, e - 1], bot[e - 1, e], grammar.NT)
-            binary(cell, bot[b, b + 1], top[b + 1, e], grammar.TN)
+                binary(cell, bot[b, b + 1], bot[b + 1, e], grammar.TT, b, e,
+                       (mbot, b, b + 1), (mbot, b + 1, e))
+            binary(cell, top[b, e - 1], bot[e - 1, e], grammar.NT, b, e,
+                   (mtop, b, e - 1), (mbot, e - 1, e))
+            binary(cell, bot[b, b + 1], top[b + 1, e], grammar.TN, b, e,
+                   (mbot, b, b + 1), (mtop, b + 1, e))
             for k in range(b + 1, e):
-                binary(cell, top[b, k], top[k, e], grammar.NN)
-            unary(top[b, e], cell, nu_p, nu_c, cl.nu_scores)
+                binary(cell, top[b, k], top[k, e], grammar.NN, b, e, (mtop, b, k), (mtop, k, e))
+            if live(mtop, b, e):
+                unary(top[b, e], cell, nu_p, nu_c, cl.nu_scores)
     return bot, top
+
+
+def _viterbi_outside(cl, words, ibot, itop):
+    """Unpruned outside pass, scattered from each parent cell to its children
+    (spans in decreasing order, so a child's parents are all done first)."""
+    n, cs = len(words), cl.cell_size
+    obot = np.full((n + 1, n + 1, cs), NEG, np.float32)
+    otop = np.full((n + 1, n + 1, cs), NEG, np.float32)
+    term = np.full((n + 1, cs), NEG, np.float32)   # terminal cells' binary share
+    otop[0, n, cl.root] = 0.0
+
+    def unary(dst, src, rules, w):
+        dst[:] = NEG
+        np.maximum.at(dst, rules[:, 1], (src[rules[:, 0]] + w).astype(np.float32))
+
+    def push(dst, parent, sib, bucket, child):
+        r, w = cl.bucket_rules[bucket], cl.bucket_scores[bucket]
+        if not r.shape[0]:
+            return
+        other = 2 if child == 1 else 1
+        np.maximum.at(dst, r[:, child], ((parent[r[:, 0]] + sib[r[:, other]]) + w).astype(np.float32))
+
+    for span in range(n, 1, -1):
+        for b in range(n - span + 1):
+            e = b + span
+            unary(obot[b, e], otop[b, e], cl.nu_rules, cl.nu_scores)
+            P = obot[b, e]
+            if span == 2:
+                push(term[b], P, ibot[b + 1, e], grammar.TT, 1)
+                push(term[b + 1], P, ibot[b, b + 1], grammar.TT, 2)
+            push(otop[b, e - 1], P, ibot[e - 1, e], grammar.NT, 1)
+            push(term[e - 1], P, itop[b, e - 1], grammar.NT, 2)
+            push(term[b], P, itop[b + 1, e], grammar.TN, 1)
+            push(otop[b + 1, e], P, ibot[b, b + 1], grammar.TN, 2)
+            for k in range(b + 1, e):
+                push(otop[b, k], P, itop[k, e], grammar.NN, 1)
+                push(otop[k, e], P, itop[b, k], grammar.NN, 2)
+    for i in range(n):
+        unary(obot[i, i + 1], otop[i, i + 1], cl.tu_rules, cl.tu_scores)
+        obot[i, i + 1] = np.maximum(obot[i, i + 1], term[i])
+    return obot, otop
+
+
+def _masks(cl, words, ibot, itop, obot, otop, thresh=-9.0):
+    """A coarse bit is live in a cell when some symbol projecting onto it has
+    inside + outside >= root + thresh (float32); span-1 bottom cells hold
+    terminals, every other cell nonterminals."""
+    n = len(words)
+    mb = np.zeros((n + 1, n + 1, cl.mask_size), np.int64)
+    mt = np.zeros_like(mb)
+    cutoff = np.float32(itop[0, n, cl.root] + np.float32(thresh))
+    ns = max(cl.n_nt, cl.n_t)
+    for b in range(n):
+        for e in range(b + 1, n + 1):
+            for m, ins, out, is_t in ((mb, ibot, obot, e == b + 1), (mt, itop, otop, False)):
+                score = (ins[b, e, :ns] + out[b, e, :ns]).astype(np.float32)
+                syms = np.nonzero(score >= cutoff)[0]
+                if is_t:
+                    field = np.where(syms < cl.n_t, cl.t_coarse[np.minimum(syms, cl.n_t - 1)], 0)
+                else:
+                    field = np.where(syms < cl.n_nt, cl.nt_coarse[np.minimum(syms, cl.n_nt - 1)], 0)
+                for f in field:
+                    m[b, e, f // 32] |= 1 << (f % 32)
+    to32 = lambda m: (m & 0xFFFFFFFF).astype(np.uint32).view(np.int32)
+    return to32(mb), to32(mt)
 
 
 def _logsum_cky(cl, words):
@@ -163,3 +254,46 @@ def test_sum_product_log_z_equals_independent_cky():
         got64 = np.log(ins64[root, cl.root]) + scales[s]
         assert abs(got64 - want) <= 1e-10 * max(1.0, abs(want)), (s, got64, want)
         assert abs(z32[s] - want) <= 1e-5 * max(1.0, abs(want)), (s, z32[s], want)
+
+
+def _cells(r, s, n):
+    """(b, e, chart row of bot(b, e), chart row of top(b, e)) for sentence s."""
+    base, tri = r.cell_off[s], n * (n + 1) // 2
+    for b in range(n):
+        for e in range(b + 1, n + 1):
+            ci = _chart_index(b, e, n)
+            yield b, e, base + ci, base + tri + ci
+
+
+def test_cascade_outside_masks_and_pruned_inside_equal_independent_cky():
+    coarse, fine = split_levels("viterbi", "medium")
+    sents = split_sentences(6, seed=34, n_words=500, mean=8, hi=12)
+    sents[1] = sents[1][:1]                       # one word: the root is -inf
+    r = oracle.run([coarse, fine], sents, mode="parse")
+    cin, cout = r.chart(0, "inside"), r.chart(0, "outside")
+    masks = r.masks(0)[0]
+    fin = r.chart(1, "inside")
+    as_bits = lambda a: a.view(np.int32)
+    live_cells = total_cells = pruned_rules = 0
+    for s, words in enumerate(sents):
+        n = len(words)
+        ibot, itop = _viterbi_cky(coarse, words)
+        obot, otop = _viterbi_outside(coarse, words, ibot, itop)
+        mbot, mtop = _masks(coarse, words, ibot, itop, obot, otop)
+        fbot, ftop = _viterbi_cky(fine, words, mbot, mtop)
+        for b, e, rb, rt in _cells(r, s, n):
+            where = (s, b, e)
+            assert np.array_equal(as_bits(cin[rb]), as_bits(ibot[b, e])), where
+            assert np.array_equal(as_bits(cin[rt]), as_bits(itop[b, e])), where
+            assert np.array_equal(as_bits(cout[rb]), as_bits(obot[b, e])), where
+            assert np.array_equal(as_bits(cout[rt]), as_bits(otop[b, e])), where
+            assert np.array_equal(masks[rb], mbot[b, e]) and np.array_equal(masks[rt], mtop[b, e]), where
+            assert np.array_equal(as_bits(fin[rb]), as_bits(fbot[b, e])), where
+            assert np.array_equal(as_bits(fin[rt]), as_bits(ftop[b, e])), where
+            live_cells += bool(np.any(mtop[b, e]))
+            total_cells += 1
+        if n > 1:
+            full_bot, _ = _viterbi_cky(fine, words)
+            pruned_rules += int(np.sum(np.isfinite(full_bot) & ~np.isfinite(fbot)))
+    # the masks prune: some cells die entirely and some fine entries are cut
+    assert 0 < live_cells < total_cells and pruned_rules > 0
