@@ -30,7 +30,7 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import small_pcfg_levels, split_levels, split_sentences, tiny_pcfg_levels
+from helpers import node_blocks, small_pcfg_levels, split_levels, split_sentences, tiny_pcfg_levels
 from puck_gb300 import grammar, synth
 
 NEG = np.float32(-np.inf)
@@ -297,3 +297,103 @@ def test_cascade_outside_masks_and_pruned_inside_equal_independent_cky():
             pruned_rules += int(np.sum(np.isfinite(full_bot) & ~np.isfinite(fbot)))
     # the masks prune: some cells die entirely and some fine entries are cut
     assert 0 < live_cells < total_cells and pruned_rules > 0
+
+
+def _check_tree(cl, words, bot, top, nodes):
+    """Re-scores a preorder node block {top or -1, bot, width, score bits}
+    against an inside chart: every rule exists, every leaf is a lexicon entry
+    of its word, and every choice attains the maximum of the backtrace's
+    candidates, ``(rule + left) + right`` and ``rule + child`` in float32
+    (CLParser.scala extractParses; ties are not told apart here)."""
+    f32 = np.float32
+    n = len(words)
+    assert nodes.shape == (max(2 * n - 1, 0), 4)
+
+    def unary_best(parent, child_cell, rules, scores, chosen):
+        sel = rules[:, 0] == parent
+        assert np.any(sel & (rules[:, 1] == chosen)), ("no unary", parent, chosen)
+        cand = (scores[sel] + child_cell[rules[sel, 1]]).astype(f32)
+        got = (scores[sel & (rules[:, 1] == chosen)][0] + child_cell[chosen]).astype(f32)
+        assert got == cand.max(), ("unary not best", parent, chosen)
+
+    def walk(p, b):
+        t, sym, width = (int(x) for x in nodes[p, :3])
+        e = b + width
+        if t != -1:
+            if width == 1:
+                unary_best(t, bot[b, e], cl.tu_rules, cl.tu_scores, sym)
+            else:
+                unary_best(t, bot[b, e], cl.nu_rules, cl.nu_scores, sym)
+        if width == 1:
+            lo, hi = cl.lex_offsets[words[b]], cl.lex_offsets[words[b] + 1]
+            assert sym in set(cl.lex_term[lo:hi].tolist()), ("not a tag of the word", b, sym)
+            assert nodes[p, 3] == bot[b, e, sym].view(np.int32)
+            return p + 1
+        lp, rp = p + 1, p + 2 * int(nodes[p + 1, 2])
+        k = b + int(nodes[lp, 2])
+        assert int(nodes[rp, 2]) == e - k
+
+        def child(q, cb, ce):
+            ct = int(nodes[q, 0])
+            return (False, int(nodes[q, 1]), bot[cb, ce]) if ct == -1 else (True, ct, top[cb, ce])
+
+        l_nt, a, lcell = child(lp, b, k)
+        r_nt, c, rcell = child(rp, k, e)
+        bucket = {(True, True): grammar.NN, (True, False): grammar.NT,
+                  (False, True): grammar.TN, (False, False): grammar.TT}[(l_nt, r_nt)]
+        rules, w = cl.bucket_rules[bucket], cl.bucket_scores[bucket]
+        hit = (rules[:, 0] == sym) & (rules[:, 1] == a) & (rules[:, 2] == c)
+        assert np.count_nonzero(hit) == 1, ("no binary rule", sym, a, c)
+        got = f32(f32(w[hit][0] + lcell[a]) + rcell[c])
+        assert nodes[p, 3] == got.view(np.int32)
+        best = f32(-np.inf)
+        splits = [(grammar.NT, top[b, e - 1], bot[e - 1, e]), (grammar.TN, bot[b, b + 1], top[b + 1, e])]
+        if width == 2:
+            splits.append((grammar.TT, bot[b, b + 1], bot[b + 1, e]))
+        splits += [(grammar.NN, top[b, j], top[j, e]) for j in range(b + 1, e)]
+        for bk, lc, rc in splits:
+            r, ww = cl.bucket_rules[bk], cl.bucket_scores[bk]
+            sel = r[:, 0] == sym
+            if np.any(sel):
+                best = max(best, ((ww[sel] + lc[r[sel, 1]]).astype(f32) + rc[r[sel, 2]]).astype(f32).max())
+        assert got == best, ("binary not best", b, e, sym)
+        q = walk(lp, b)
+        assert q == rp
+        return walk(rp, k)
+
+    assert int(nodes[0, 0]) == cl.root and int(nodes[0, 2]) == n
+    assert walk(0, 0) == nodes.shape[0]
+
+
+def test_viterbi_trees_are_argmax_derivations():
+    cl = tiny_pcfg_levels()[0]
+    sents = [s for s in _sentences(cl, 16, seed=35, lo=2, hi=12)]
+    r = oracle.run([cl], sents, mode="parse")
+    checked = 0
+    for s, nodes in enumerate(node_blocks(r.trees(), [len(x) for x in sents])):
+        bot, top = _viterbi_cky(cl, sents[s])
+        if not np.isfinite(top[0, len(sents[s]), cl.root]):
+            continue
+        _check_tree(cl, sents[s], bot, top, nodes)
+        checked += 1
+        # negative controls on a copy: a score one ulp off, a wrong symbol
+        for row, col, delta in ((0, 3, 1), (1, 1, 1)):
+            bad = nodes.copy()
+            bad[row, col] += delta
+            with pytest.raises(AssertionError):
+                _check_tree(cl, sents[s], bot, top, bad)
+    assert checked >= len(sents) // 2
+
+
+def test_cascade_trees_are_argmax_derivations_of_the_pruned_chart():
+    coarse, fine = split_levels("viterbi", "medium")
+    sents = split_sentences(5, seed=36, n_words=500, mean=9, hi=14)
+    r = oracle.run([coarse, fine], sents, mode="parse")
+    blocks = node_blocks(r.trees(), [len(x) for x in sents])
+    for s, words in enumerate(sents):
+        ibot, itop = _viterbi_cky(coarse, words)
+        obot, otop = _viterbi_outside(coarse, words, ibot, itop)
+        mbot, mtop = _masks(coarse, words, ibot, itop, obot, otop)
+        fbot, ftop = _viterbi_cky(fine, words, mbot, mtop)
+        assert np.isfinite(ftop[0, len(words), fine.root])
+        _check_tree(fine, words, fbot, ftop, blocks[s])
