@@ -41,39 +41,67 @@ def _chart_index(b, e, n):
     return b + sp * n - sp * (sp - 1) // 2
 
 
-def _viterbi_cky(cl, words, mbot=None, mtop=None):
+class _Semiring:
+    """Max in float32 (Viterbi, bit-exact with the oracle) or log-add in
+    float64 (sum-product, log space).  Rule weights are taken in log space:
+    a Real level's linear float32 weights are logged in float64."""
+
+    def __init__(self, dtype, acc, linear_weights):
+        self.dtype, self.acc, self.linear = dtype, acc, linear_weights
+
+    def w(self, x):
+        x = np.asarray(x)
+        return np.log(x.astype(np.float64)) if self.linear else x.astype(self.dtype)
+
+
+VIT = _Semiring(np.float32, np.maximum, False)
+
+
+def _log(cl):
+    return _Semiring(np.float64, np.logaddexp, cl.semiring == "real")
+
+
+_BUCKET_NAME = {grammar.NN: "NN", grammar.NT: "NT", grammar.TN: "TN", grammar.TT: "TT"}
+
+
+def _live(m, b, e):
+    return m is None or bool(np.any(m[b, e]))
+
+
+def _gate(cl, job, syms, m):
+    """Rows whose target symbol's segment meets the cell mask ``m``."""
+    j = cl.jobs[job]
+    return np.any(j["seg_bits"][j["tgt_seg"][syms]] & m, axis=1)
+
+
+def _inside(cl, words, sr, mbot=None, mtop=None):
     """Inside pass.  ``mbot``/``mtop`` (int32[n+1, n+1, mask_size]) are the
     coarse level's masks; None runs unpruned."""
     n, cs = len(words), cl.cell_size
-    bot = np.full((n + 1, n + 1, cs), NEG, np.float32)
-    top = np.full((n + 1, n + 1, cs), NEG, np.float32)
-    nu_p, nu_c = cl.nu_rules[:, 0], cl.nu_rules[:, 1]
-    tu_p, tu_c = cl.tu_rules[:, 0], cl.tu_rules[:, 1]
-    names = {grammar.NN: "in_NN", grammar.NT: "in_NT", grammar.TN: "in_TN", grammar.TT: "in_TT"}
+    zero = sr.dtype(-np.inf)
+    bot = np.full((n + 1, n + 1, cs), zero, sr.dtype)
+    top = np.full((n + 1, n + 1, cs), zero, sr.dtype)
+    wb = [sr.w(x) for x in cl.bucket_scores]
+    wnu, wtu = sr.w(cl.nu_scores), sr.w(cl.tu_scores)
 
-    def live(m, b, e):
-        return m is None or bool(np.any(m[b, e]))
-
-    def unary(dst, src, p, c, w):
-        dst[:] = NEG
-        np.maximum.at(dst, p, (src[c] + w).astype(np.float32))
+    def unary(dst, src, rules, w):
+        dst[:] = zero
+        sr.acc.at(dst, rules[:, 0], (src[rules[:, 1]] + w).astype(sr.dtype))
 
     for i, w in enumerate(words):
         lo, hi = cl.lex_offsets[w], cl.lex_offsets[w + 1]
         bot[i, i + 1, cl.lex_term[lo:hi]] = cl.lex_score[lo:hi]
-        if live(mtop, i, i + 1):
-            unary(top[i, i + 1], bot[i, i + 1], tu_p, tu_c, cl.tu_scores)
+        if _live(mtop, i, i + 1):
+            unary(top[i, i + 1], bot[i, i + 1], cl.tu_rules, wtu)
 
     def binary(dst, left, right, bucket, b, e, lcell, rcell):
-        r, w = cl.bucket_rules[bucket], cl.bucket_scores[bucket]
-        if not r.shape[0] or not (live(lcell[0], *lcell[1:]) and live(rcell[0], *rcell[1:])):
+        r, w = cl.bucket_rules[bucket], wb[bucket]
+        if not r.shape[0] or not (_live(*lcell) and _live(*rcell)):
             return
         if mbot is not None:
-            job = cl.jobs[names[bucket]]
-            gate = job["seg_bits"][job["tgt_seg"][r[:, 0]]]
-            keep = np.any(gate & mbot[b, e], axis=1)
+            keep = _gate(cl, "in_" + _BUCKET_NAME[bucket], r[:, 0], mbot[b, e])
             r, w = r[keep], w[keep]
-        np.maximum.at(dst, r[:, 0], ((left[r[:, 1]] + right[r[:, 2]]) + w).astype(np.float32))
+        sr.acc.at(dst, r[:, 0], ((left[r[:, 1]] + right[r[:, 2]]) + w).astype(sr.dtype))
 
     for span in range(2, n + 1):
         for b in range(n - span + 1):
@@ -88,50 +116,74 @@ def _viterbi_cky(cl, words, mbot=None, mtop=None):
                    (mbot, b, b + 1), (mtop, b + 1, e))
             for k in range(b + 1, e):
                 binary(cell, top[b, k], top[k, e], grammar.NN, b, e, (mtop, b, k), (mtop, k, e))
-            if live(mtop, b, e):
-                unary(top[b, e], cell, nu_p, nu_c, cl.nu_scores)
+            if _live(mtop, b, e):
+                unary(top[b, e], cell, cl.nu_rules, wnu)
     return bot, top
 
 
-def _viterbi_outside(cl, words, ibot, itop):
-    """Unpruned outside pass, scattered from each parent cell to its children
-    (spans in decreasing order, so a child's parents are all done first)."""
+def _outside(cl, words, ibot, itop, sr, mbot=None, mtop=None):
+    """Outside pass, scattered from each parent cell to its children (spans
+    in decreasing order, so a child's parents are all done first).  Under
+    masks a parent's share reaches a child when the parent's bottom cell and
+    the sibling's cell hold a live bit and the child's cell mask meets the
+    segment of the child's symbol in the rotated job (out_L_* / out_R_*);
+    unaries run from live top cells only."""
     n, cs = len(words), cl.cell_size
-    obot = np.full((n + 1, n + 1, cs), NEG, np.float32)
-    otop = np.full((n + 1, n + 1, cs), NEG, np.float32)
-    term = np.full((n + 1, cs), NEG, np.float32)   # terminal cells' binary share
+    zero = sr.dtype(-np.inf)
+    obot = np.full((n + 1, n + 1, cs), zero, sr.dtype)
+    otop = np.full((n + 1, n + 1, cs), zero, sr.dtype)
+    term = np.full((n + 1, cs), zero, sr.dtype)   # terminal cells' binary share
     otop[0, n, cl.root] = 0.0
+    wb = [sr.w(x) for x in cl.bucket_scores]
+    wnu, wtu = sr.w(cl.nu_scores), sr.w(cl.tu_scores)
 
     def unary(dst, src, rules, w):
-        dst[:] = NEG
-        np.maximum.at(dst, rules[:, 1], (src[rules[:, 0]] + w).astype(np.float32))
+        dst[:] = zero
+        sr.acc.at(dst, rules[:, 1], (src[rules[:, 0]] + w).astype(sr.dtype))
 
-    def push(dst, parent, sib, bucket, child):
-        r, w = cl.bucket_rules[bucket], cl.bucket_scores[bucket]
-        if not r.shape[0]:
+    def push(dst, child_cell, parent, sib, sib_cell, bucket, child):
+        r, w = cl.bucket_rules[bucket], wb[bucket]
+        if not r.shape[0] or not _live(*sib_cell):
             return
+        if child_cell[0] is not None:
+            m, cb, ce = child_cell
+            keep = _gate(cl, "out_%s_%s" % ("L" if child == 1 else "R", _BUCKET_NAME[bucket]),
+                         r[:, child], m[cb, ce])
+            r, w = r[keep], w[keep]
         other = 2 if child == 1 else 1
-        np.maximum.at(dst, r[:, child], ((parent[r[:, 0]] + sib[r[:, other]]) + w).astype(np.float32))
+        sr.acc.at(dst, r[:, child], ((parent[r[:, 0]] + sib[r[:, other]]) + w).astype(sr.dtype))
 
     for span in range(n, 1, -1):
         for b in range(n - span + 1):
             e = b + span
-            unary(obot[b, e], otop[b, e], cl.nu_rules, cl.nu_scores)
+            if _live(mtop, b, e):
+                unary(obot[b, e], otop[b, e], cl.nu_rules, wnu)
+            if not _live(mbot, b, e):
+                continue
             P = obot[b, e]
             if span == 2:
-                push(term[b], P, ibot[b + 1, e], grammar.TT, 1)
-                push(term[b + 1], P, ibot[b, b + 1], grammar.TT, 2)
-            push(otop[b, e - 1], P, ibot[e - 1, e], grammar.NT, 1)
-            push(term[e - 1], P, itop[b, e - 1], grammar.NT, 2)
-            push(term[b], P, itop[b + 1, e], grammar.TN, 1)
-            push(otop[b + 1, e], P, ibot[b, b + 1], grammar.TN, 2)
+                push(term[b], (mbot, b, b + 1), P, ibot[b + 1, e], (mbot, b + 1, e), grammar.TT, 1)
+                push(term[b + 1], (mbot, b + 1, e), P, ibot[b, b + 1], (mbot, b, b + 1), grammar.TT, 2)
+            push(otop[b, e - 1], (mtop, b, e - 1), P, ibot[e - 1, e], (mbot, e - 1, e), grammar.NT, 1)
+            push(term[e - 1], (mbot, e - 1, e), P, itop[b, e - 1], (mtop, b, e - 1), grammar.NT, 2)
+            push(term[b], (mbot, b, b + 1), P, itop[b + 1, e], (mtop, b + 1, e), grammar.TN, 1)
+            push(otop[b + 1, e], (mtop, b + 1, e), P, ibot[b, b + 1], (mbot, b, b + 1), grammar.TN, 2)
             for k in range(b + 1, e):
-                push(otop[b, k], P, itop[k, e], grammar.NN, 1)
-                push(otop[k, e], P, itop[b, k], grammar.NN, 2)
+                push(otop[b, k], (mtop, b, k), P, itop[k, e], (mtop, k, e), grammar.NN, 1)
+                push(otop[k, e], (mtop, k, e), P, itop[b, k], (mtop, b, k), grammar.NN, 2)
     for i in range(n):
-        unary(obot[i, i + 1], otop[i, i + 1], cl.tu_rules, cl.tu_scores)
-        obot[i, i + 1] = np.maximum(obot[i, i + 1], term[i])
+        if _live(mtop, i, i + 1):
+            unary(obot[i, i + 1], otop[i, i + 1], cl.tu_rules, wtu)
+        obot[i, i + 1] = sr.acc(obot[i, i + 1], term[i])
     return obot, otop
+
+
+def _viterbi_cky(cl, words, mbot=None, mtop=None):
+    return _inside(cl, words, VIT, mbot, mtop)
+
+
+def _viterbi_outside(cl, words, ibot, itop):
+    return _outside(cl, words, ibot, itop, VIT)
 
 
 def _masks(cl, words, ibot, itop, obot, otop, thresh=-9.0):
@@ -160,40 +212,8 @@ def _masks(cl, words, ibot, itop, obot, otop, thresh=-9.0):
 
 def _logsum_cky(cl, words):
     """log Z in float64 log space over the same cell recursion."""
-    n, cs = len(words), cl.cell_size
-    ninf = -np.inf
-    bot = np.full((n + 1, n + 1, cs), ninf)
-    top = np.full((n + 1, n + 1, cs), ninf)
-    lw = [np.log(s.astype(np.float64)) for s in cl.bucket_scores]
-    lnu = np.log(cl.nu_scores.astype(np.float64))
-    ltu = np.log(cl.tu_scores.astype(np.float64))
-
-    def unary(dst, src, rules, w):
-        dst[:] = ninf
-        np.logaddexp.at(dst, rules[:, 0], src[rules[:, 1]] + w)
-
-    for i, w in enumerate(words):
-        lo, hi = cl.lex_offsets[w], cl.lex_offsets[w + 1]
-        bot[i, i + 1, cl.lex_term[lo:hi]] = cl.lex_score[lo:hi].astype(np.float64)
-        unary(top[i, i + 1], bot[i, i + 1], cl.tu_rules, ltu)
-
-    def binary(dst, left, right, bucket):
-        r = cl.bucket_rules[bucket]
-        if r.shape[0]:
-            np.logaddexp.at(dst, r[:, 0], left[r[:, 1]] + right[r[:, 2]] + lw[bucket])
-
-    for span in range(2, n + 1):
-        for b in range(n - span + 1):
-            e = b + span
-            cell = bot[b, e]
-            if span == 2:
-                binary(cell, bot[b, b + 1], bot[b + 1, e], grammar.TT)
-            binary(cell, top[b, e - 1], bot[e - 1, e], grammar.NT)
-            binary(cell, bot[b, b + 1], top[b + 1, e], grammar.TN)
-            for k in range(b + 1, e):
-                binary(cell, top[b, k], top[k, e], grammar.NN)
-            unary(top[b, e], cell, cl.nu_rules, lnu)
-    return top[0, n, cl.root]
+    _, top = _inside(cl, words, _log(cl))
+    return top[0, len(words), cl.root]
 
 
 def _sentences(cl, n, seed, lo=1, hi=9):
@@ -397,3 +417,55 @@ def test_cascade_trees_are_argmax_derivations_of_the_pruned_chart():
         fbot, ftop = _viterbi_cky(fine, words, mbot, mtop)
         assert np.isfinite(ftop[0, len(words), fine.root])
         _check_tree(fine, words, fbot, ftop, blocks[s])
+
+
+def _coarse_marginals(cl, ins, out, log_z, is_terminal_cell):
+    """Posterior mass of each coarse symbol in one cell half (float64)."""
+    nk, proj = (cl.n_t, cl.t_coarse) if is_terminal_cell else (cl.n_nt, cl.nt_coarse)
+    m = np.zeros(cl.n_coarse)
+    np.add.at(m, proj[:nk], np.exp(ins[:nk] + out[:nk] - log_z))
+    return m
+
+
+def test_sum_product_cascade_marginals_equal_independent_cky():
+    """The FP64 oracle's MBR cell scores are posterior coarse marginals in
+    scaled space: ``score * exp(iscale + oscale - iscale[root cell])`` must
+    equal the best coarse marginal of a float64 log-space inside/outside
+    under the same masks (relative 1e-6: the score is returned in float32),
+    and its symbol must be the argmax wherever the top two differ by more
+    than 1e-5 relative.  The lexicon's per-word normalisers cancel between
+    inside * outside and the root."""
+    coarse, fine = split_levels("real", "medium")
+    sents = split_sentences(5, seed=37, n_words=500, mean=8, hi=12)
+    r32 = oracle.run([coarse, fine], sents, mode="parse")
+    m, isc, osc = r32.masks(0)
+    r64 = oracle.OracleRun([oracle.OracleLevel(l) for l in (coarse, fine)], sents, precision=64)
+    r64.set_final_masks(m, isc, osc)
+    assert r64.run("parse") == 0
+    score, sym = r64.mbr_cells()
+    lg = _log(fine)
+    cells = decided = 0
+    for s, words in enumerate(sents):
+        n = len(words)
+        ibot, itop = _viterbi_cky(coarse, words)
+        obot, otop = _viterbi_outside(coarse, words, ibot, itop)
+        mbot, mtop = _masks(coarse, words, ibot, itop, obot, otop)
+        fb, ft = _inside(fine, words, lg, mbot, mtop)
+        ob, ot = _outside(fine, words, fb, ft, lg, mbot, mtop)
+        log_z = ft[0, n, fine.root]
+        assert np.isfinite(log_z)
+        root_row = r32.cell_off[s] + n * (n + 1) // 2 + _chart_index(0, n, n)
+        for b, e, rb, rt in _cells(r32, s, n):
+            assert np.array_equal(m[rb], mbot[b, e]) and np.array_equal(m[rt], mtop[b, e])
+            for row, ins, out, term in ((rb, fb[b, e], ob[b, e], e == b + 1), (rt, ft[b, e], ot[b, e], False)):
+                marg = _coarse_marginals(fine, ins, out, log_z, term)
+                got = float(score[row]) * np.exp(float(isc[row]) + float(osc[row]) - float(isc[root_row]))
+                assert abs(got - marg.max()) <= 1e-6 * marg.max() + 1e-12, (s, b, e, got, marg.max())
+                two = np.sort(marg)[-2:]
+                if two[1] - two[0] > 1e-5 * two[1]:
+                    assert sym[row] == int(np.argmax(marg)), (s, b, e)
+                    decided += 1
+                cells += 1
+        # the root cell's top half holds the whole mass on the root's symbol
+        assert np.isclose(_coarse_marginals(fine, ft[0, n], ot[0, n], log_z, False).max(), 1.0)
+    assert decided > cells // 2
