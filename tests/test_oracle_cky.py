@@ -469,3 +469,78 @@ def test_sum_product_cascade_marginals_equal_independent_cky():
         # the root cell's top half holds the whole mass on the root's symbol
         assert np.isclose(_coarse_marginals(fine, ft[0, n], ot[0, n], log_z, False).max(), 1.0)
     assert decided > cells // 2
+
+
+def test_logsum_log_z_equals_independent_cky():
+    """LogSum (RuleSemiring.scala LogSumRuleSemiring: log-add with zero
+    -1e6) computes log Z directly in float32: within 1e-5 relative of the
+    float64 log-space CKY, on the unpruned tiny grammar."""
+    cl = tiny_pcfg_levels("logsum")[0]
+    sents = _sentences(cl, 10, seed=38, lo=2, hi=10)
+    z = oracle.run([cl], sents, mode="partitions").partitions().astype(np.float64)
+    for s, words in enumerate(sents):
+        want = _logsum_cky(cl, words)
+        assert np.isfinite(want)
+        assert abs(z[s] - want) <= 1e-5 * max(1.0, abs(want)), (s, z[s], want)
+
+
+def _mbr_tree(n, cell_score, cell_sym, bot_row, top_row, iscale, oscale):
+    """extractMBRParses (CLParser.scala:589-686) restated in float32 from the
+    per-cell best marginals: unscale each half by
+    exp((iscale + oscale) - iscale[root]), NaN -> 0, clamp at 1; a cell takes
+    its unary when it spans two words or more or its top score passes 0.4;
+    the best split wins by strict '>' starting from 0 and the first split."""
+    f32 = np.float32
+    root_row = top_row(0, n)
+    best, split, uu = {}, {}, {}
+    for span in range(1, n + 1):
+        for b in range(n - span + 1):
+            e = b + span
+            halves = []
+            for row in (top_row(b, e), bot_row(b, e)):
+                at = f32(f32(iscale[row] + oscale[row]) - iscale[root_row])
+                v = f32(cell_score[row] * f32(np.exp(np.float64(at))))
+                v = f32(0.0) if np.isnan(v) else v
+                halves.append(min(v, f32(1.0)))
+            top, bot = halves
+            uu[b, e] = (b + 1 < e) or top > f32(0.4)
+            best[b, e] = f32(top + bot) if uu[b, e] else bot
+            if span > 1:
+                bs, bss = b + 1, f32(0.0)
+                for k in range(b + 1, e):
+                    sc = f32(best[b, k] + best[k, e])
+                    if sc > bss:
+                        bs, bss = k, sc
+                split[b, e] = bs
+                best[b, e] = f32(best[b, e] + bss)
+    out = []
+
+    def emit(b, e):
+        out.append([int(cell_sym[top_row(b, e)]) if uu[b, e] else -1, int(cell_sym[bot_row(b, e)]),
+                    e - b, int(best[b, e].view(np.int32))])
+        if e - b > 1:
+            emit(b, split[b, e])
+            emit(split[b, e], e)
+
+    emit(0, n)
+    return np.array(out, np.int32)
+
+
+def test_mbr_trees_equal_restated_extraction():
+    coarse, fine = split_levels("real", "medium")
+    sents = split_sentences(8, seed=39, n_words=500, mean=10, hi=16)
+    sents[2] = sents[2][:1]
+    r = oracle.run([coarse, fine], sents, mode="parse")
+    _, isc, osc = r.masks(0)
+    score, sym = r.mbr_cells()
+    blocks = node_blocks(r.trees(), [len(x) for x in sents])
+    unary_spans = 0
+    for s, words in enumerate(sents):
+        n = len(words)
+        base, tri = r.cell_off[s], n * (n + 1) // 2
+        want = _mbr_tree(n, score, sym, lambda b, e: base + _chart_index(b, e, n),
+                         lambda b, e: base + tri + _chart_index(b, e, n), isc, osc)
+        assert np.array_equal(blocks[s], want), s
+        unary_spans += int(np.sum((want[:, 2] == 1) & (want[:, 0] != -1)))
+    # some one-word spans pass the 0.4 threshold and take their unary
+    assert unary_spans > 0
