@@ -153,6 +153,18 @@ def cpu_baseline(levels, sents, sample: int):
                       f"fine inside, backtrace; {dt:.1f}s"}, r
 
 
+def reference_work(r, value: float) -> dict:
+    """The reference's work measure on the CPU-baseline sample: (rule, split)
+    applications its binary queues run in the last level's inside pass
+    (rows queued per rule block times the block's rules, counted by the
+    oracle), per sentence and at this run's sentences/s."""
+    apps = r.rule_apps(len(r.levels) - 1, "inside") / max(len(r.lengths), 1)
+    return {"rule_apps_per_sentence": round(apps), "rule_apps_per_s": float(f"{apps * value:.4g}"),
+            "sample": f"the {len(r.lengths)} sentences of the CPU baseline",
+            "note": "reference-equivalent CKY rule applications (fine inside, after pruning); "
+                    "not the roofline's split-factored work"}
+
+
 def parity(path, sents, batch_nodes, r, device: int):
     """The GPU's results on the CPU-baseline sample against the oracle's
     (the oracle run ``r`` of that sample): the sample's trees taken from the
@@ -420,6 +432,10 @@ def run_ours(args):
     if rank == 0 and world == 1:
         if args.cpu_sample > 0:
             out["cpu_baseline"], r_cpu = cpu_baseline(levels, sents, args.cpu_sample)
+            try:
+                out["reference_work"] = reference_work(r_cpu, value)
+            except Exception as exc:  # a report, never a reason to lose the line
+                out["reference_work"] = {"unavailable": str(exc)[:160]}
             out["parity"] = parity(path, sents, nodes, r_cpu, local)
             log(f"parity: {out['parity']}")
         if args.plain_sample > 0:

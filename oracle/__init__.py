@@ -73,6 +73,8 @@ def lib():
         L.po_run_get_partition_scales.argtypes = [P, I, P]
         L.po_run_corner_drops.argtypes = [P, I]
         L.po_run_corner_drops.restype = ctypes.c_int64
+        L.po_run_rule_apps.argtypes = [P, I, I]
+        L.po_run_rule_apps.restype = ctypes.c_int64
         L.po_run_get_trees.argtypes = [P, P]
         L.po_run_get_partitions.argtypes = [P, P]
         L.po_run_get_mbr.argtypes = [P, P, P]
@@ -220,6 +222,11 @@ class OracleRun:
 
     def corner_drops(self, level: int) -> int:
         return int(lib().po_run_corner_drops(self.h, level))
+
+    def rule_apps(self, level: int, which: str = "inside") -> int:
+        """(rule, split) applications of the reference's binary queues in
+        one pass of one level: rows queued per rule block times its rules."""
+        return int(lib().po_run_rule_apps(self.h, level, 0 if which == "inside" else 1))
 
     def trees(self) -> np.ndarray:
         n = int(lib().po_run_num_nodes(self.h))

@@ -151,6 +151,10 @@ template <class F> struct Engine {
   std::vector<F> iscale, oscale;     // scale buffers of this level's charts
   std::vector<double> partition_scales;
   int64_t corner_drops = 0;          // atomic_min writes of a value >= +0.0 that were dropped
+  // (rule, split) applications the reference's queues run: rows queued for a
+  // block times the block's rules, summed per pass (0 inside, 1 outside)
+  int64_t rule_apps[2] = {0, 0};
+  int apps_pass = 0;
 
   Engine(const Level& l, const Batch& b, const MaskIn& m, bool mg, int th)
       : L(l), B(b), M(m), merged(mg), S{l.semiring}, threads(th) {
@@ -248,6 +252,10 @@ template <class F> struct Engine {
       for (size_t i = 0; i < q.size(); ++i) if (i == 0 || q[i].p != q[i - 1].p) gstart.push_back(i);
       gstart.push_back(q.size());
       int seg_lo = merged ? 0 : k, seg_hi = merged ? J.nseg : k + 1;
+      int64_t block_rules = 0;
+      for (size_t sub = 0; sub < J.sub_seg.size(); ++sub)
+        if (J.sub_seg[sub] >= seg_lo && J.sub_seg[sub] < seg_hi) block_rules += J.sub_off[sub + 1] - J.sub_off[sub];
+      rule_apps[apps_pass] += (int64_t)q.size() * block_rules;
       const int64_t ngroups = (int64_t)gstart.size() - 1;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(threads)
       for (int64_t g = 0; g < ngroups; ++g) {
@@ -351,6 +359,7 @@ template <class F> struct Engine {
   }
 
   void run_inside() {
+    apps_pass = 0;
     int64_t nc = B.num_cells();
     inside.assign((size_t)nc * L.cell_size, S.zero());
     outside.assign((size_t)nc * L.cell_size, S.zero());
@@ -370,6 +379,7 @@ template <class F> struct Engine {
   }
 
   void run_outside() {
+    apps_pass = 1;
     // setRootScores
     for (int s = 0; s < B.nsent; ++s) cellp(outside, B.top(s, 0, B.len[s]))[L.root] = S.one();
     unary_update(OUT_NU, B.max_len, outside, BOT, TOP, oscale);
@@ -602,6 +612,7 @@ struct LevelResult {
   std::vector<float> iscale, oscale;          // scales this level produced for the next
   std::vector<double> partition_scales;
   int64_t corner_drops = 0;
+  int64_t rule_apps[2] = {0, 0};
   bool has_outside = false;
 };
 
@@ -636,6 +647,8 @@ void store(LevelResult& r, Engine<F>& E, bool outside) {
   }
   r.partition_scales = E.partition_scales;
   r.corner_drops = E.corner_drops;
+  r.rule_apps[0] = E.rule_apps[0];
+  r.rule_apps[1] = E.rule_apps[1];
   r.has_outside = outside;
 }
 
@@ -838,6 +851,9 @@ void po_run_get_partition_scales(void* rv, int level, double* out) {
 }
 
 int64_t po_run_corner_drops(void* rv, int level) { return ((Run*)rv)->res[level].corner_drops; }
+
+// pass 0 = inside, 1 = outside
+int64_t po_run_rule_apps(void* rv, int level, int pass) { return ((Run*)rv)->res[level].rule_apps[pass & 1]; }
 
 void po_run_get_trees(void* rv, int32_t* nodes) {
   Run* R = (Run*)rv;

@@ -74,9 +74,10 @@ def _gate(cl, job, syms, m):
     return np.any(j["seg_bits"][j["tgt_seg"][syms]] & m, axis=1)
 
 
-def _inside(cl, words, sr, mbot=None, mtop=None):
+def _inside(cl, words, sr, mbot=None, mtop=None, apps=None):
     """Inside pass.  ``mbot``/``mtop`` (int32[n+1, n+1, mask_size]) are the
-    coarse level's masks; None runs unpruned."""
+    coarse level's masks; None runs unpruned.  ``apps`` (a one-item list)
+    accumulates the (rule, split) applications made."""
     n, cs = len(words), cl.cell_size
     zero = sr.dtype(-np.inf)
     bot = np.full((n + 1, n + 1, cs), zero, sr.dtype)
@@ -101,6 +102,8 @@ def _inside(cl, words, sr, mbot=None, mtop=None):
         if mbot is not None:
             keep = _gate(cl, "in_" + _BUCKET_NAME[bucket], r[:, 0], mbot[b, e])
             r, w = r[keep], w[keep]
+        if apps is not None:
+            apps[0] += r.shape[0]
         sr.acc.at(dst, r[:, 0], ((left[r[:, 1]] + right[r[:, 2]]) + w).astype(sr.dtype))
 
     for span in range(2, n + 1):
@@ -544,3 +547,59 @@ def test_mbr_trees_equal_restated_extraction():
         unary_spans += int(np.sum((want[:, 2] == 1) & (want[:, 0] != -1)))
     # some one-word spans pass the 0.4 threshold and take their unary
     assert unary_spans > 0
+
+
+def test_rule_application_counts():
+    """The oracle's count of (rule, split) applications, the reference's
+    work measure ("CKY rule-apps"): unpruned, a closed form over the split
+    ranges of each bucket; pruned, the independent CKY's own count."""
+    cl = tiny_pcfg_levels()[0]
+    sents = _sentences(cl, 6, seed=40, lo=1, hi=9)
+    r = oracle.run([cl], sents, mode="inside_outside")
+    nr = {k: cl.bucket_rules[k].shape[0] for k in (grammar.NN, grammar.NT, grammar.TN, grammar.TT)}
+    want_in = want_out = 0
+    for words in sents:
+        n = len(words)
+        for span in range(2, n + 1):
+            cells = n - span + 1
+            want_in += cells * (nr[grammar.NN] * (span - 1) + nr[grammar.NT] + nr[grammar.TN]
+                                + (nr[grammar.TT] if span == 2 else 0))
+        for b in range(n):
+            for e in range(b + 1, n + 1):
+                right, left = n - e, b          # parents ending after e / starting before b
+                # the cell as a nonterminal child (top half)
+                want_out += nr[grammar.NN] * (right + left) + nr[grammar.NT] * (e < n) + nr[grammar.TN] * (b > 0)
+                if e == b + 1:                  # as a terminal child (bottom half)
+                    want_out += nr[grammar.TT] * ((e < n) + (b > 0)) + nr[grammar.NT] * left + nr[grammar.TN] * right
+    assert r.rule_apps(0, "inside") == want_in
+    assert r.rule_apps(0, "outside") == want_out
+
+    coarse, fine = split_levels("viterbi", "medium")
+    sents = split_sentences(4, seed=41, n_words=500, mean=8, hi=12)
+    r = oracle.run([coarse, fine], sents, mode="parse")
+    apps, full = [0], [0]
+    for words in sents:
+        ibot, itop = _viterbi_cky(coarse, words)
+        obot, otop = _viterbi_outside(coarse, words, ibot, itop)
+        mbot, mtop = _masks(coarse, words, ibot, itop, obot, otop)
+        _inside(fine, words, VIT, mbot, mtop, apps)
+        _inside(fine, words, VIT, None, None, full)
+    assert r.rule_apps(1, "inside") == apps[0] < full[0]
+
+
+def test_bench_cpu_baseline_reports_reference_work():
+    """bench.py's CPU-baseline leg and its rule-application report, run on a
+    small cascade exactly as the bench calls them (host only)."""
+    import json
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    levels = split_levels("viterbi", "medium")
+    sents = split_sentences(8, seed=42, n_words=500, mean=8, hi=12)
+    base, r = bench.cpu_baseline(levels, sents, 6)
+    assert base["kind"] == "port" and base["value"] > 0
+    rep = bench.reference_work(r, 1000.0)
+    assert rep["rule_apps_per_sentence"] == round(r.rule_apps(1, "inside") / 6) > 0
+    assert abs(rep["rule_apps_per_s"] / (r.rule_apps(1, "inside") / 6 * 1000.0) - 1) < 1e-3
+    json.dumps(rep)
