@@ -603,3 +603,59 @@ def test_bench_cpu_baseline_reports_reference_work():
     assert rep["rule_apps_per_sentence"] == round(r.rule_apps(1, "inside") / 6) > 0
     assert abs(rep["rule_apps_per_s"] / (r.rule_apps(1, "inside") / 6 * 1000.0) - 1) < 1e-3
     json.dumps(rep)
+
+
+class _ArtifactLevel:
+    """The attributes the independent CKY reads, taken from one level of a
+    compiled ``.grz`` artifact (rule-order job tables, lexicon, coarse maps)."""
+
+    def __init__(self, info):
+        a = info.arrays
+        for k in ("semiring", "n_nt", "n_t", "cell_size", "mask_size", "n_coarse", "root"):
+            setattr(self, k, getattr(info, k))
+        names = [_BUCKET_NAME[b] for b in (grammar.NN, grammar.NT, grammar.TN, grammar.TT)]
+        self.bucket_rules = [np.stack([a[f"in_{n}/tgt"], a[f"in_{n}/ia"], a[f"in_{n}/ib"]], 1) for n in names]
+        self.bucket_scores = [a[f"in_{n}/score"] for n in names]
+        self.nu_rules = np.stack([a["in_NU/tgt"], a["in_NU/osrc"]], 1)
+        self.nu_scores = a["in_NU/score"]
+        self.tu_rules = np.stack([a["in_TU/tgt"], a["in_TU/osrc"]], 1)
+        self.tu_scores = a["in_TU/score"]
+        self.lex_offsets, self.lex_term, self.lex_score = a["lex_off"], a["lex_term"], a["lex_score"]
+        self.nt_coarse, self.t_coarse = a["nt_coarse"], a["t_coarse"]
+        self.jobs = {}
+        for j in grammar.JOBS:
+            self.jobs[j[0]] = {"seg_bits": a[f"{j[0]}/seg_bits"].reshape(-1, self.mask_size),
+                               "tgt_seg": a[f"{j[0]}/tgt_seg"]}
+
+
+def test_wsj_golden_fixture_equals_independent_cky():
+    """The committed wsj_0 -> wsj_1 fixture (the reference's own Berkeley
+    grammars, every rule kept): its coarse masks are the independent CKY's
+    bit for bit, and each of its trees is an argmax derivation of the
+    independent pruned fine chart."""
+    import os
+    from puck_gb300 import grz
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    levels = [_ArtifactLevel(l) for l in grz.read_sequence(os.path.join(here, "wsj01_cascade_viterbi.grz"),
+                                                            load_arrays=True)]
+    data = np.load(os.path.join(here, "wsj01_cascade_viterbi.npz"))
+    off, words, masks = data["offsets"], data["words"], data["masks"]
+    sents = [words[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+    blocks = node_blocks(data["trees"], [len(s) for s in sents])
+    coarse, fine = levels
+    base = 0
+    for s, w in enumerate(sents):
+        n = len(w)
+        ibot, itop = _viterbi_cky(coarse, w)
+        obot, otop = _viterbi_outside(coarse, w, ibot, itop)
+        mbot, mtop = _masks(coarse, w, ibot, itop, obot, otop)
+        tri = n * (n + 1) // 2
+        for b in range(n):
+            for e in range(b + 1, n + 1):
+                ci = _chart_index(b, e, n)
+                assert np.array_equal(masks[base + ci], mbot[b, e]), (s, b, e)
+                assert np.array_equal(masks[base + tri + ci], mtop[b, e]), (s, b, e)
+        base += 2 * tri
+        fbot, ftop = _inside(fine, w, VIT, mbot, mtop)
+        assert np.isfinite(ftop[0, n, fine.root])
+        _check_tree(fine, w, fbot, ftop, blocks[s])
