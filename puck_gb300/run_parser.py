@@ -12,9 +12,10 @@ labels; a sentence that fails prints ``(())`` (RunParser.scala:100-107).
 
 Like the reference, sentences stream through a batching service -- here the
 library's continuous-batching server -- and results are written in order.
-Only newline sentence segmentation and whitespace tokenization exist here
-(the reference's trained segmenter and treebank tokenizer are epic
-components); other values are accepted with a warning.
+``--sentences`` and ``--tokens`` take the reference's values and defaults
+(``trained`` and ``default``: running text is split into sentences and
+tokenized the Penn Treebank way); see :mod:`puck_gb300.preprocess` for what
+stands in for epic's segmenters and tokenizer.
 """
 from __future__ import annotations
 
@@ -23,8 +24,9 @@ import collections
 import re
 import sys
 import time
-from typing import Iterable, List, Optional, TextIO
+from typing import Callable, Iterable, List, Optional, TextIO
 
+from . import preprocess
 from .parser import debinarize
 from .server import CLServer
 
@@ -44,18 +46,9 @@ def _bool(v: str) -> bool:
     return v.lower() in ("true", "1", "yes")
 
 
-def sentences(src: TextIO) -> Iterable[str]:
-    """Newline segmentation; blank lines are skipped (RunParser.scala:92)."""
-    for line in src:
-        if line.strip():
-            yield line.rstrip("\n")
-
-
-def tokens(sentence: str) -> List[str]:
-    return sentence.split()
-
-
-def parse_stream(server: CLServer, src: TextIO, sink: TextIO, max_length: int, window: int = 4096) -> int:
+def parse_stream(server: CLServer, src: TextIO, sink: TextIO, max_length: int, window: int = 4096,
+                 segment: Callable[[TextIO], Iterable[str]] = preprocess.newline_sentences,
+                 tokenize: Callable[[str], List[str]] = preprocess.whitespace_tokens) -> int:
     """Submits sentences as they are read and writes results in input order;
     at most ``window`` results are outstanding.  Returns the count."""
     pending = collections.deque()
@@ -72,8 +65,10 @@ def parse_stream(server: CLServer, src: TextIO, sink: TextIO, max_length: int, w
         else:
             sink.write(debinarize(res.get()).render(words) + "\n")
 
-    for sent in sentences(src):
-        words = tokens(sent)
+    for sent in segment(src):
+        words = tokenize(sent)
+        if not words:
+            continue
         n += 1
         fut = server.submit(words) if len(words) < max_length else None
         pending.append((words, fut))
@@ -93,15 +88,15 @@ def main(argv: Optional[List[str]] = None) -> int:
     ap.add_argument("--mem", type=parse_mem, default=parse_mem("3g"))
     ap.add_argument("--profile", type=_bool, nargs="?", const=True, default=False)
     ap.add_argument("--device", default="0")
-    ap.add_argument("--sentences", default="newline")
-    ap.add_argument("--tokens", default="whitespace")
+    ap.add_argument("--sentences", default="trained")
+    ap.add_argument("--tokens", default="default")
     ap.add_argument("--outputSuffix", default=".parsed")
     a = ap.parse_args(argv)
-    if a.sentences.lower() != "newline":
-        print(f"run_parser: sentence segmenter {a.sentences!r} is not available; using newline",
-              file=sys.stderr)
-    if a.tokens.lower() not in ("whitespace", "none"):
-        print(f"run_parser: tokenizer {a.tokens!r} is not available; using whitespace", file=sys.stderr)
+    try:
+        segment = preprocess.sentence_segmenter(a.sentences)
+        tokenize = preprocess.tokenizer(a.tokens)
+    except ValueError as exc:
+        ap.error(str(exc))
     device = int(a.device) if a.device.isdigit() else 0
     # sentences with maxLength tokens or more never reach the parser
     server = CLServer(a.grammar, max_alloc_size=a.mem, device=device, max_length=min(max(a.maxLength - 1, 1), 256),
@@ -110,10 +105,11 @@ def main(argv: Optional[List[str]] = None) -> int:
     total = 0
     try:
         if not a.files:
-            total += parse_stream(server, sys.stdin, sys.stdout, a.maxLength)
+            total += parse_stream(server, sys.stdin, sys.stdout, a.maxLength,
+                                  segment=segment, tokenize=tokenize)
         for f in a.files:
             with open(f, encoding="utf-8") as src, open(f + a.outputSuffix, "w", encoding="utf-8") as sink:
-                total += parse_stream(server, src, sink, a.maxLength)
+                total += parse_stream(server, src, sink, a.maxLength, segment=segment, tokenize=tokenize)
     finally:
         server.close()
     wall = time.time() - t0

@@ -145,7 +145,8 @@ def test_run_parser_end_to_end_matches_oracle(tmp_path):
     text[3] = text[3] + " not_a_word"
     inp = tmp_path / "in.txt"
     inp.write_text("\n".join(text) + "\n")
-    r = _module("puck_gb300.run_parser", "--grammar", out, "--maxLength", "19", "--mem", "2g", str(inp))
+    r = _module("puck_gb300.run_parser", "--grammar", out, "--maxLength", "19", "--mem", "2g",
+                "--sentences", "newline", "--tokens", "whitespace", str(inp))
     assert r.returncode == 0, r.stderr
     lines = (tmp_path / "in.txt.parsed").read_text().splitlines()
     assert len(lines) == len(text)
