@@ -12,8 +12,8 @@ epic's segmenters and tokenizers by ``--sentences`` and ``--tokens``).
   dotted abbreviations.  Sentences never cross a blank line.
 * ``whitespace`` / ``none`` tokens: split on whitespace.
 * ``treebank`` / ``default`` tokens: the Penn Treebank conventions that the
-  Berkeley grammars' lexicons are written in (`````` and ``''``
-  quotes, ``-LRB-`` style brackets, ``n't`` and ``'s`` clitics split off,
+  Berkeley grammars' lexicons are written in (double quotes as two
+  backquotes or two apostrophes, ``-LRB-`` style brackets, ``n't`` and ``'s`` clitics split off,
   ``ca n't``, ``gon na``, a sentence-final period split off -- repeated after
   an abbreviation, as in ``U.S. .``).  epic's TreebankTokenizer, the
   reference's, is a generated lexer that is not in the tree, so agreement
