@@ -160,3 +160,21 @@ def test_run_parser_end_to_end_matches_oracle(tmp_path):
             continue
         ref = oracle.run(levels, [s], mode="parse").trees()
         assert lines[i] == debinarize(nodes_to_viterbi_tree(ref, data)).render(words)
+
+
+@pytest.mark.skipif(not os.path.exists(TEXT + "/wsj_1.gr.binary"), reason="reference text grammars absent")
+def test_treebank_tokens_of_running_text_are_in_the_wsj_vocabulary():
+    """run_parser's default front end (rule-based segmenter, treebank
+    tokenizer) turns running English into the lexicon's own token forms;
+    whitespace tokens of the same text mostly miss it."""
+    from puck_gb300.preprocess import segment, treebank_tokens
+    gs = berkeley.read_cascade([TEXT + "/wsj_0.gr", TEXT + "/wsj_1.gr"])
+    vocab = set(gs[1].words)
+    text = ("The company said it expects revenue to rise 5% next year, but analysts weren't convinced. "
+            '"We can\'t predict the market," Mr. Jones said (in an interview). Shares of the U.S. unit '
+            "fell $1.25 to $30. It's the firm's third quarterly loss -- and investors' patience is thin...")
+    sents = segment(text)
+    assert len(sents) == 4
+    toks = [t for s in sents for t in treebank_tokens(s)]
+    assert [t for t in toks if t not in vocab] == []
+    assert sum(t not in vocab for s in sents for t in s.split()) >= 10
