@@ -169,3 +169,49 @@ def test_compile_grammar_from_a_host_without_python(tmp_path):
     py = str(tmp_path / "py.grz")
     assert compile_grammar.main(["--textGrammarPrefix", f"{c}:{f}", "--grammar", py]) == 0
     _same_archives(out, py)
+
+
+def _c_kind(ctype: str) -> str:
+    t = ctype.strip()
+    if "*" in t or "[" in t:
+        return "ADDRESS"
+    base = t.replace("const", "").split()[-1]
+    return {"int64_t": "JAVA_LONG", "size_t": "JAVA_LONG", "int32_t": "JAVA_INT", "puck_status": "JAVA_INT",
+            "int": "JAVA_INT", "float": "JAVA_FLOAT", "double": "JAVA_DOUBLE"}[base]
+
+
+def test_panama_binding_in_integration_doc_matches_header():
+    """The JVM binding shown for maintainers cannot be compiled here (no
+    JDK); its downcall descriptors are checked against the C declarations
+    instead: every bound name exists, with the same argument count, argument
+    and return kinds, and puck_options' layout has the header's fields in
+    order and its 48 bytes."""
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = open(os.path.join(root, "include", "puck_gpu.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", " ", hdr, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(puck_\w+)\s*\(([^)]*)\)\s*;", hdr):
+        ret, name, args = m.group(1).split(";")[-1].split("}")[-1].strip(), m.group(2), m.group(3).strip()
+        params = [] if args in ("", "void") else [a.rsplit(None, 1)[0] if not a.strip().endswith("]")
+                                                  else a for a in args.split(",")]
+        protos[name] = (None if ret == "void" else _c_kind(ret), [_c_kind(p) for p in params])
+    doc = open(os.path.join(root, "INTEGRATION.md")).read()
+    java = doc[doc.index("```java"):]
+    java = java[:java.index("```", 7)]
+    bound = re.findall(r'h\("(puck_\w+)",\s*FunctionDescriptor\.(ofVoid|of)\(([^)]*)\)\)', java, flags=re.S)
+    assert len(bound) >= 8
+    for name, form, items in bound:
+        kinds = [k.strip() for k in items.split(",") if k.strip()]
+        ret = None if form == "ofVoid" else kinds.pop(0)
+        assert name in protos, name
+        assert (ret, kinds) == protos[name], (name, (ret, kinds), protos[name])
+    fields = re.search(r"typedef struct puck_options \{(.*?)\} puck_options;", hdr, flags=re.S).group(1)
+    c_fields = [(_c_kind(f.rsplit(None, 1)[0]), f.rsplit(None, 1)[1]) for f in
+                (x.strip() for x in fields.split(";")) if f]
+    layout = re.search(r"structLayout\((.*?)\);", java, flags=re.S).group(1)
+    j_fields = re.findall(r"(JAVA_\w+)\.withName\(\"(\w+)\"\)", layout)
+    assert j_fields == c_fields
+    size = {"JAVA_LONG": 8, "JAVA_INT": 4, "JAVA_FLOAT": 4}
+    pad = sum(int(x) for x in re.findall(r"paddingLayout\((\d+)\)", layout))
+    assert sum(size[k] for k, _ in j_fields) + pad == 48
