@@ -134,6 +134,11 @@ def load(build: bool = True) -> ctypes.CDLL:
         L.puck_server_lanes.restype = I
         L.puck_last_error.argtypes = [ctypes.c_char_p, ctypes.c_size_t]
         L.puck_last_error.restype = ctypes.c_size_t
+        L.puck_default_compile_options.argtypes = [P]
+        L.puck_compile_grammar.argtypes = [ctypes.c_char_p, ctypes.c_char_p, P]
+        L.puck_compile_grammar.restype = I
+        L.puck_mbr_decode_static.argtypes = [P, P, P, P, I, P, P]
+        L.puck_mbr_decode_static.restype = I
         _lib = L
         return L
 

@@ -215,3 +215,40 @@ def test_panama_binding_in_integration_doc_matches_header():
     size = {"JAVA_LONG": 8, "JAVA_INT": 4, "JAVA_FLOAT": 4}
     pad = sum(int(x) for x in re.findall(r"paddingLayout\((\d+)\)", layout))
     assert sum(size[k] for k, _ in j_fields) + pad == 48
+
+
+def test_ctypes_binding_matches_header():
+    """Every entry point the Python side binds has the header's argument
+    count and kinds (pointer, 32-bit, 64-bit, float) and return kind."""
+    import ctypes
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    hdr = re.sub(r"/\*.*?\*/", " ", open(os.path.join(root, "include", "puck_gpu.h")).read(), flags=re.S)
+    protos = {}
+    for m in re.finditer(r"([A-Za-z_][\w\s\*]*?)\b(puck_\w+)\s*\(([^)]*)\)\s*;", hdr):
+        ret, name, args = m.group(1).split(";")[-1].split("}")[-1].strip(), m.group(2), m.group(3).strip()
+        params = [] if args in ("", "void") else [a if a.strip().endswith("]") else a.rsplit(None, 1)[0]
+                                                  for a in args.split(",")]
+        protos[name] = (None if ret == "void" else _c_kind(ret), [_c_kind(p) for p in params])
+
+    def kind(t):
+        if t is None:
+            return None
+        if t in (ctypes.c_void_p, ctypes.c_char_p) or issubclass(t, ctypes._Pointer):
+            return "ADDRESS"
+        return {ctypes.c_int32: "JAVA_INT", ctypes.c_int64: "JAVA_LONG", ctypes.c_size_t: "JAVA_LONG",
+                ctypes.c_float: "JAVA_FLOAT", ctypes.c_double: "JAVA_DOUBLE"}[t]
+
+    L = _lib.load()
+    assert set(_lib.EXPORTS) == set(protos)
+    for name in _lib.EXPORTS:
+        f = getattr(L, name)
+        assert f.argtypes is not None, name
+        want_ret, want_args = protos[name]
+        got_ret = None if f.restype is None else kind(f.restype)
+        if want_ret is None:
+            # ctypes' default restype is c_int; a void function may keep it
+            assert got_ret in (None, "JAVA_INT"), name
+        else:
+            assert got_ret == want_ret, (name, got_ret, want_ret)
+        assert [kind(t) for t in f.argtypes] == want_args, (name, [kind(t) for t in f.argtypes], want_args)
