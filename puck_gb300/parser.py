@@ -108,6 +108,11 @@ class CLParserData:
     def write_sequence(path: str, compiled_levels) -> None:
         grz.write_sequence(path, compiled_levels)
 
+    # the reference's names (CLParser.scala:1302-1317; CLParserData.isViterbi)
+    readSequence = read_sequence
+    writeSequence = write_sequence
+    isViterbi = is_viterbi
+
     def nt_label(self, i: int) -> str:
         return self.info.coarse_names[int(self.nt_coarse[i])]
 
@@ -286,6 +291,10 @@ class CLParser:
         ids = [self.word_ids(s) for s in sentences]
         words, offsets, _ = pack_sentences(ids)
         self.inside_outside_ids(words, offsets)
+
+    # the reference's names (CLParser.scala:60,71)
+    insideOutside = inside_outside
+    isViterbi = is_viterbi
 
     # -- device state of the last call (single batch only) ----------------
     def debug_num_cells(self) -> int:

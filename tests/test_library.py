@@ -252,3 +252,19 @@ def test_ctypes_binding_matches_header():
         else:
             assert got_ret == want_ret, (name, got_ret, want_ret)
         assert [kind(t) for t in f.argtypes] == want_args, (name, [kind(t) for t in f.argtypes], want_args)
+
+
+def test_python_mirror_keeps_the_reference_names():
+    """CLParser / CLParserData carry the reference's method names beside the
+    Python ones (parse, partitions, insideOutside, release, isViterbi,
+    readSequence, writeSequence)."""
+    from puck_gb300.parser import CLParser, CLParserData
+    for name in ("parse", "partitions", "insideOutside", "release", "isViterbi"):
+        assert hasattr(CLParser, name), name
+    assert CLParser.insideOutside is CLParser.inside_outside
+    assert CLParser.isViterbi is CLParser.is_viterbi
+    for name in ("readSequence", "writeSequence", "isViterbi"):
+        assert hasattr(CLParserData, name), name
+    from helpers import small_pcfg_levels, write_grz
+    data = CLParserData.readSequence(write_grz(small_pcfg_levels(), "names_check"))
+    assert len(data) == 1 and data[0].isViterbi and data[0].is_viterbi
