@@ -686,3 +686,28 @@ def test_golden_fixture_equals_independent_cky(case):
             want = ftop[0, n, fine.root]
             got = float(data["partitions"][s])
             assert abs(got - want) <= 1e-5 * max(1.0, abs(want)), (s, got, want)
+
+
+def test_pruned_fine_outside_chart_equals_independent_cky():
+    """The fine level's Viterbi outside pass under the coarse masks (the
+    chart the GPU tests compare bit for bit): the independent scatter form
+    with the rotated jobs' gating gives the oracle's chart bit for bit."""
+    coarse, fine = split_levels("viterbi", "medium")
+    sents = split_sentences(5, seed=43, n_words=500, mean=9, hi=13)
+    r = oracle.run([coarse, fine], sents, mode="inside_outside")
+    fin, fout = r.chart(1, "inside"), r.chart(1, "outside")
+    bits = lambda a: a.view(np.int32)
+    live = 0
+    for s, words in enumerate(sents):
+        n = len(words)
+        ibot, itop = _viterbi_cky(coarse, words)
+        obot, otop = _viterbi_outside(coarse, words, ibot, itop)
+        mbot, mtop = _masks(coarse, words, ibot, itop, obot, otop)
+        fb, ft = _inside(fine, words, VIT, mbot, mtop)
+        ob, ot = _outside(fine, words, fb, ft, VIT, mbot, mtop)
+        for b, e, rb, rt in _cells(r, s, n):
+            assert np.array_equal(bits(fin[rb]), bits(fb[b, e])) and np.array_equal(bits(fin[rt]), bits(ft[b, e]))
+            assert np.array_equal(bits(fout[rb]), bits(ob[b, e])), (s, b, e, "bot")
+            assert np.array_equal(bits(fout[rt]), bits(ot[b, e])), (s, b, e, "top")
+            live += int(np.isfinite(ot[b, e]).sum())
+    assert live > 0
