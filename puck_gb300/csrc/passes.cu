@@ -25,7 +25,9 @@
 // 16 x 16 sub-tiles, an 8 x 4 lane grid over each, four-split groups staged
 // per warp, four-rule records), for both the max-plus and the sum-product
 // semiring and for both passes.  The host picks the mode per level and per
-// span launch.
+// span launch.  Within mode 0, an ungated job (no coarse mask, not LogSum)
+// with few rules per target scans its distinct child pairs instead of its
+// targets (gather_pairmajor).
 //
 // Reference semantics restated (dlwh/puck paths):
 //   gating        CLParser.scala:845-855,885-901 (segment bits vs cell mask, child "any")
