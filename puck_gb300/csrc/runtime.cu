@@ -62,7 +62,8 @@ struct ZipReader {
       const uint16_t method = u16(&data[cd + 10]);
       const uint32_t csize = u32(&data[cd + 20]);
       const uint16_t nl = u16(&data[cd + 28]), xl = u16(&data[cd + 30]), cl = u16(&data[cd + 32]);
-      const uint32_t lho = u32(&data[cd + 42]);
+      const size_t lho = u32(&data[cd + 42]);
+      if (cd + 46 + nl > data.size()) throw PuckError{PUCK_ERR_BAD_GRAMMAR, path + ": corrupt central directory"};
       std::string name(reinterpret_cast<const char*>(&data[cd + 46]), nl);
       cd += 46 + nl + xl + cl;
       if (name.size() >= 8 && name.compare(name.size() - 8, 8, ".program") == 0) continue;  // never decoded
@@ -265,7 +266,9 @@ void load_grammar(puck_grammar* g, const std::string& path) {
       std::memcpy(a.tag, p + 4, 4);
       std::memcpy(&a.count, p + 8, 8);
       size_t esz = (std::strncmp(a.tag, "i8", 2) == 0) ? 8 : 4;
-      if (16 + a.count * esz > e.second.second) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "truncated " + e.first};
+      // the count comes from the file: bound it before any arithmetic on it
+      if (a.count < 0 || (uint64_t)a.count > (e.second.second - 16) / esz)
+        throw PuckError{PUCK_ERR_BAD_GRAMMAR, "truncated " + e.first};
       a.bytes.assign(p + 16, p + 16 + a.count * esz);
       L.arrays[e.first.substr(pre.size())] = std::move(a);
     }

@@ -89,6 +89,55 @@ def test_bad_artifacts_fail_cleanly(tmp_path):
     assert st.value == 2
 
 
+def _patched(tmp_path, name, patch):
+    """A copy of a valid archive with ``patch(bytearray, eocd, cd)`` applied."""
+    import struct
+    data = bytearray(open(os.path.join(GOLDEN, "tiny_pcfg_viterbi.grz"), "rb").read())
+    eocd = data.rindex(b"PK\x05\x06")
+    cd = struct.unpack_from("<I", data, eocd + 16)[0]
+    patch(data, eocd, cd)
+    p = tmp_path / name
+    p.write_bytes(bytes(data))
+    return str(p).encode()
+
+
+def test_corrupt_offsets_and_counts_fail_cleanly(tmp_path):
+    """Fields read from the file are bounded before use: an entry name
+    running past the end, a local-header offset near 2^32, an array element
+    count that is negative or overflows its byte size."""
+    import struct
+    L = _lib.load()
+    st = ctypes.c_int32(0)
+
+    def last_entry_long_name(d, eocd, cd):
+        n = struct.unpack_from("<H", d, eocd + 10)[0]
+        for _ in range(n - 1):                      # walk to the last central-directory entry
+            nl, xl, cl = struct.unpack_from("<HHH", d, cd + 28)
+            cd += 46 + nl + xl + cl
+        struct.pack_into("<H", d, cd + 28, 0xFFFF)
+
+    def huge_local_offset(d, eocd, cd):
+        struct.pack_into("<I", d, cd + 42, 0xFFFFFFF0)
+
+    for name, patch, msg in (("name.grz", last_entry_long_name, "corrupt central directory"),
+                             ("lho.grz", huge_local_offset, "corrupt local header")):
+        assert not L.puck_grammar_load(_patched(tmp_path, name, patch), ctypes.byref(st))
+        assert st.value == 2 and msg in _lib.last_error(), _lib.last_error()
+
+    import zipfile
+    src = os.path.join(GOLDEN, "tiny_pcfg_viterbi.grz")
+    for count in (-1, -(1 << 62), 1 << 62, (1 << 63) - 1):
+        q = tmp_path / f"count{count & 0xff}.grz"
+        with zipfile.ZipFile(src) as zin, zipfile.ZipFile(q, "w", zipfile.ZIP_STORED) as zout:
+            for info in zin.infolist():
+                data = zin.read(info.filename)
+                if info.filename == "parser-0/arrays/in_NN/w":
+                    data = data[:8] + struct.pack("<q", count) + data[16:]
+                zout.writestr(zipfile.ZipInfo(info.filename, date_time=(1980, 1, 1, 0, 0, 0)), data)
+        assert not L.puck_grammar_load(str(q).encode(), ctypes.byref(st))
+        assert st.value == 2 and "truncated parser-0/arrays/in_NN/w" in _lib.last_error(), _lib.last_error()
+
+
 def test_build_flags_target_sm103a():
     assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
 
