@@ -125,11 +125,39 @@ void validate_level(const HostLevel& L) {
     for (int64_t k = 0; k < c; ++k)
       if (v[k] < 0 || v[k] >= hi) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "index out of range in " + n};
   };
+  // offset tables the device walks: 0 first, never decreasing, ending at the
+  // element count of the table they index
+  auto offsets = [&](const std::string& n, int64_t last) {
+    int64_t c = 0;
+    if (L.arrays.at(n).tag[1] == '8') {
+      const long long* v = L.get<long long>(n, "i8", &c);
+      for (int64_t k = 0; k < c; ++k)
+        if ((k == 0 && v[0] != 0) || (k > 0 && v[k] < v[k - 1]) || (k == c - 1 && v[k] != last))
+          throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad offsets in " + n};
+    } else {
+      const int* v = L.get<int>(n, "i4", &c);
+      for (int64_t k = 0; k < c; ++k)
+        if ((k == 0 && v[0] != 0) || (k > 0 && v[k] < v[k - 1]) || (k == c - 1 && v[k] != last))
+          throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad offsets in " + n};
+    }
+  };
+  // weights: any value but NaN (-inf is a legal log weight)
+  auto no_nan = [&](const std::string& n) {
+    int64_t c = 0;
+    const float* v = L.get<float>(n, "f4", &c);
+    for (int64_t k = 0; k < c; ++k)
+      if (std::isnan(v[k])) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "NaN weight in " + n};
+  };
   need("nt_coarse", "i4", L.n_nt);
   need("t_coarse", "i4", L.n_t);
   range("nt_coarse", L.n_coarse);
   range("t_coarse", L.n_coarse);
   if (L.root < 0 || L.root >= L.n_nt) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "root out of range"};
+  // coarse member lists first: the pair-table checks below read them
+  need("nt_mem_off", "i4", L.n_coarse + 1);
+  need("t_mem_off", "i4", L.n_coarse + 1);
+  offsets("nt_mem_off", L.n_nt);
+  offsets("t_mem_off", L.n_t);
   static const bool tgt_t[puck::NJOBS] = {false, false, false, false, false, false, false, true, true, false, true, true};
   static const bool a_t[puck::NJOBS] = {false, false, true, true, false, false, false, false, false, true, false, true};
   static const bool b_t[puck::NJOBS] = {false, true, false, true, false, false, true, false, false, false, true, false};
@@ -143,6 +171,7 @@ void validate_level(const HostLevel& L) {
     if (rp[0] != 0 || rp[nr - 1] != nab) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad rowptr for " + n};
     for (int64_t k = 0; k + 1 < nr; ++k)
       if (rp[k + 1] < rp[k]) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad rowptr for " + n};
+    no_nan(n + "/w");
     const int* ab = L.get<int>(n + "/ab", "i4", nullptr);
     const int amax = a_t[j] ? L.n_t : L.n_nt, bmax = b_t[j] ? L.n_t : L.n_nt;
     for (int64_t k = 0; k < nab; ++k) {
@@ -161,6 +190,10 @@ void validate_level(const HostLevel& L) {
       const int64_t nbp = need(n + "/blk_ptr", "i4", nbs + 1);
       const int64_t npr = need(n + "/pair_rule", "i4", nab);
       need(n + "/pair_w", "f4", nab);
+      no_nan(n + "/pair_w");
+      // whole tables before the walk below indexes with them
+      offsets(n + "/pair_blk", nbs);
+      offsets(n + "/blk_ptr", npr);
       const int* pk = L.get<int>(n + "/pair_key", "i4", nullptr);
       const int* pb = L.get<int>(n + "/pair_blk", "i4", nullptr);
       const int* bs = L.get<int>(n + "/blk_seg", "i4", nullptr);
@@ -198,11 +231,11 @@ void validate_level(const HostLevel& L) {
     const int64_t nr = need(n + "/rowptr", "i4", (ut[j] ? L.n_t : L.n_nt) + 1);
     const int* rp = L.get<int>(n + "/rowptr", "i4", nullptr);
     const int64_t ns = need(n + "/src", "i4", rp[nr - 1]);
+    offsets(n + "/rowptr", ns);
     need(n + "/w", "f4", ns);
+    no_nan(n + "/w");
     range(n + "/src", us[j] ? L.n_t : L.n_nt);
   }
-  need("nt_mem_off", "i4", L.n_coarse + 1);
-  need("t_mem_off", "i4", L.n_coarse + 1);
   need("nt_mem", "i4", L.n_nt);
   need("t_mem", "i4", L.n_t);
   range("nt_mem", L.n_nt);
@@ -211,12 +244,18 @@ void validate_level(const HostLevel& L) {
   const long long* lo = L.get<long long>("lex_off", "i8", nullptr);
   need("lex_term", "i4", lo[nlo - 1]);
   need("lex_score", "f4", lo[nlo - 1]);
+  offsets("lex_off", lo[nlo - 1]);
+  no_nan("lex_score");
   range("lex_term", L.n_t);
   const int64_t nvo = need("v_off", "i4", 6LL * L.n_nt + 1);
   const int* vo = L.get<int>("v_off", "i4", nullptr);
   need("v_left", "i4", vo[nvo - 1]);
   need("v_score", "f4", vo[nvo - 1]);
   need("v_right", "i4", vo[nvo - 1]);
+  offsets("v_off", vo[nvo - 1]);
+  no_nan("v_score");
+  range("v_left", std::max(L.n_nt, L.n_t));
+  range("v_right", std::max(L.n_nt, L.n_t));
 }
 
 void load_grammar(puck_grammar* g, const std::string& path) {

@@ -317,3 +317,105 @@ def test_python_mirror_keeps_the_reference_names():
     from helpers import small_pcfg_levels, write_grz
     data = CLParserData.readSequence(write_grz(small_pcfg_levels(), "names_check"))
     assert len(data) == 1 and data[0].isViterbi and data[0].is_viterbi
+
+
+def _with_array(tmp_path, name, entry, fn):
+    """A copy of a valid archive whose array ``entry`` (of level 0) has its
+    elements passed through ``fn(numpy array) -> numpy array``."""
+    import zipfile
+    import numpy as np
+    src = os.path.join(GOLDEN, "tiny_pcfg_viterbi.grz")
+    q = tmp_path / name
+    with zipfile.ZipFile(src) as zin, zipfile.ZipFile(q, "w", zipfile.ZIP_STORED) as zout:
+        for info in zin.infolist():
+            data = zin.read(info.filename)
+            if info.filename == f"parser-0/arrays/{entry}":
+                tag = data[4:8].rstrip(b"\0 ").decode()
+                dt = {"i4": np.int32, "i8": np.int64, "f4": np.float32}[tag[:2]]
+                vals = fn(np.frombuffer(data[16:], dt).copy()).astype(dt)
+                data = data[:16] + vals.tobytes()
+            zout.writestr(zipfile.ZipInfo(info.filename, date_time=(1980, 1, 1, 0, 0, 0)), data)
+    return str(q).encode()
+
+
+def test_tables_the_device_walks_are_validated_at_load(tmp_path):
+    """Offset tables that are not 0-based and non-decreasing, backtrace
+    symbols out of range and NaN weights are refused when the archive is
+    loaded, before any device table is built from them."""
+    import numpy as np
+    L = _lib.load()
+    st = ctypes.c_int32(0)
+
+    def swap_middle(v):
+        k = len(v) // 2
+        v[k], v[k + 1] = v[k + 1] + 1, v[k]   # a step down inside the table
+        return v
+
+    def first(x):
+        def f(v):
+            v[0] = x
+            return v
+        return f
+
+    cases = [
+        ("lex_off", swap_middle, "bad offsets in lex_off"),
+        ("v_off", swap_middle, "bad offsets in v_off"),
+        ("nt_mem_off", first(1), "bad offsets in nt_mem_off"),
+        ("in_NU/rowptr", swap_middle, "bad offsets in in_NU/rowptr"),
+        ("in_NN/pair_blk", swap_middle, "bad offsets in in_NN/pair_blk"),
+        ("in_NN/blk_ptr", swap_middle, "bad offsets in in_NN/blk_ptr"),
+        ("v_left", first(1 << 20), "index out of range in v_left"),
+        ("v_right", first(-1), "index out of range in v_right"),
+        ("in_NN/w", first(np.nan), "NaN weight in in_NN/w"),
+        ("lex_score", first(np.nan), "NaN weight in lex_score"),
+    ]
+    for entry, fn, msg in cases:
+        p = _with_array(tmp_path, entry.replace("/", "_") + ".grz", entry, fn)
+        assert not L.puck_grammar_load(p, ctypes.byref(st)), entry
+        assert st.value == 2 and msg in _lib.last_error(), (entry, _lib.last_error())
+    # -inf stays a legal log weight
+    p = _with_array(tmp_path, "neginf.grz", "in_NN/w", first(-np.inf))
+    g = L.puck_grammar_load(p, ctypes.byref(st))
+    assert g and st.value == 0
+    L.puck_grammar_free(g)
+
+
+def test_randomly_corrupted_archives_load_or_fail_cleanly(tmp_path):
+    """Seeded corruption of a valid archive (truncation, bit flips, byte
+    noise, zeroed runs): every load either succeeds or returns
+    PUCK_ERR_BAD_GRAMMAR with a message; none crashes."""
+    import random
+    L = _lib.load()
+    st = ctypes.c_int32(0)
+    src = open(os.path.join(GOLDEN, "split_cascade_viterbi.grz"), "rb").read()
+    rng = random.Random(2026)
+    outcomes = {0: 0, 2: 0}
+    for it in range(150):
+        b = bytearray(src)
+        kind = it % 4
+        if kind == 0:
+            b = b[:rng.randrange(len(b))]
+        elif kind == 1:
+            for _ in range(rng.randint(1, 4)):
+                b[rng.randrange(len(b))] ^= 1 << rng.randrange(8)
+        elif kind == 2:
+            for _ in range(rng.randint(20, 200)):
+                b[rng.randrange(len(b))] = rng.randrange(256)
+        else:
+            s = rng.randrange(len(b))
+            n = min(rng.randint(4, 4096), len(b) - s)
+            b[s:s + n] = bytes(n)
+        p = tmp_path / f"c{it}.grz"
+        p.write_bytes(bytes(b))
+        g = L.puck_grammar_load(str(p).encode(), ctypes.byref(st))
+        assert st.value in (0, 2), (it, st.value)
+        assert bool(g) == (st.value == 0)
+        if g:
+            out = (ctypes.c_int32 * 8)()
+            for lv in range(L.puck_grammar_num_levels(g)):
+                assert L.puck_grammar_level_info(g, lv, out) == 0
+            L.puck_grammar_free(g)
+        else:
+            assert _lib.last_error()
+        outcomes[st.value] += 1
+    assert outcomes[2] > 100
