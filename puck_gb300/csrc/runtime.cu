@@ -292,6 +292,9 @@ void load_grammar(puck_grammar* g, const std::string& path) {
     L.n_words = geti("n_words");
     if (L.mask_size > puck::kMaxMask || L.n_coarse > puck::kMaxCoarse)
       throw PuckError{PUCK_ERR_BAD_GRAMMAR, "too many coarse symbols"};
+    // every coarse id needs a bit in a cell's mask words
+    if (L.n_coarse < 1 || L.mask_size < 1 || L.n_coarse > 32 * L.mask_size)
+      throw PuckError{PUCK_ERR_BAD_GRAMMAR, "mask size does not cover the coarse symbols"};
     if (L.cell_size % 32 != 0 || L.cell_size < std::max(L.n_nt, L.n_t))
       throw PuckError{PUCK_ERR_BAD_GRAMMAR, "bad cell size"};
     if (std::max(L.n_nt, L.n_t) > 65535) throw PuckError{PUCK_ERR_BAD_GRAMMAR, "more than 65535 symbols"};

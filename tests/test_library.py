@@ -373,6 +373,20 @@ def test_tables_the_device_walks_are_validated_at_load(tmp_path):
         p = _with_array(tmp_path, entry.replace("/", "_") + ".grz", entry, fn)
         assert not L.puck_grammar_load(p, ctypes.byref(st)), entry
         assert st.value == 2 and msg in _lib.last_error(), (entry, _lib.last_error())
+    # a header whose mask words cannot hold every coarse symbol
+    import zipfile
+    q = tmp_path / "mask.grz"
+    with zipfile.ZipFile(os.path.join(GOLDEN, "tiny_pcfg_viterbi.grz")) as zin, \
+            zipfile.ZipFile(q, "w", zipfile.ZIP_STORED) as zout:
+        for info in zin.infolist():
+            data = zin.read(info.filename)
+            if info.filename == "parser-0/header":
+                lines = [l for l in data.decode().splitlines() if l]
+                data = "".join((f"n_coarse 40\n" if l.startswith("n_coarse ") else l + "\n")
+                               for l in lines).encode()
+            zout.writestr(zipfile.ZipInfo(info.filename, date_time=(1980, 1, 1, 0, 0, 0)), data)
+    assert not L.puck_grammar_load(str(q).encode(), ctypes.byref(st))
+    assert st.value == 2 and "mask size does not cover" in _lib.last_error(), _lib.last_error()
     # -inf stays a legal log weight
     p = _with_array(tmp_path, "neginf.grz", "in_NN/w", first(-np.inf))
     g = L.puck_grammar_load(p, ctypes.byref(st))
