@@ -68,13 +68,18 @@ def _live(m, b, e):
     return m is None or bool(np.any(m[b, e]))
 
 
-def _gate(cl, job, syms, m):
-    """Rows whose target symbol's segment meets the cell mask ``m``."""
+def _gate(cl, job, syms, m, merged=False):
+    """Rows whose target symbol's segment meets the cell mask ``m``.  A
+    merged level (a middle level of a cascade) runs every rule as one block,
+    gated by segment 0's bits (CLParser.scala:783-785)."""
     j = cl.jobs[job]
+    if merged:
+        hit = j["seg_bits"].shape[0] > 0 and bool(np.any(j["seg_bits"][0] & m))
+        return np.full(len(syms), hit)
     return np.any(j["seg_bits"][j["tgt_seg"][syms]] & m, axis=1)
 
 
-def _inside(cl, words, sr, mbot=None, mtop=None, apps=None):
+def _inside(cl, words, sr, mbot=None, mtop=None, apps=None, merged=False):
     """Inside pass.  ``mbot``/``mtop`` (int32[n+1, n+1, mask_size]) are the
     coarse level's masks; None runs unpruned.  ``apps`` (a one-item list)
     accumulates the (rule, split) applications made."""
@@ -100,7 +105,7 @@ def _inside(cl, words, sr, mbot=None, mtop=None, apps=None):
         if not r.shape[0] or not (_live(*lcell) and _live(*rcell)):
             return
         if mbot is not None:
-            keep = _gate(cl, "in_" + _BUCKET_NAME[bucket], r[:, 0], mbot[b, e])
+            keep = _gate(cl, "in_" + _BUCKET_NAME[bucket], r[:, 0], mbot[b, e], merged)
             r, w = r[keep], w[keep]
         if apps is not None:
             apps[0] += r.shape[0]
@@ -124,7 +129,7 @@ def _inside(cl, words, sr, mbot=None, mtop=None, apps=None):
     return bot, top
 
 
-def _outside(cl, words, ibot, itop, sr, mbot=None, mtop=None):
+def _outside(cl, words, ibot, itop, sr, mbot=None, mtop=None, merged=False):
     """Outside pass, scattered from each parent cell to its children (spans
     in decreasing order, so a child's parents are all done first).  Under
     masks a parent's share reaches a child when the parent's bottom cell and
@@ -151,7 +156,7 @@ def _outside(cl, words, ibot, itop, sr, mbot=None, mtop=None):
         if child_cell[0] is not None:
             m, cb, ce = child_cell
             keep = _gate(cl, "out_%s_%s" % ("L" if child == 1 else "R", _BUCKET_NAME[bucket]),
-                         r[:, child], m[cb, ce])
+                         r[:, child], m[cb, ce], merged)
             r, w = r[keep], w[keep]
         other = 2 if child == 1 else 1
         sr.acc.at(dst, r[:, child], ((parent[r[:, 0]] + sib[r[:, other]]) + w).astype(sr.dtype))
@@ -711,3 +716,40 @@ def test_pruned_fine_outside_chart_equals_independent_cky():
             assert np.array_equal(bits(fout[rt]), bits(ot[b, e])), (s, b, e, "top")
             live += int(np.isfinite(ot[b, e]).sum())
     assert live > 0
+
+
+def test_three_level_cascade_with_a_merged_middle_level():
+    """coarse -> fine -> fine (a self-cascade, as the reference's own
+    CLParserTest builds): the middle level runs merged blocks under the
+    coarse masks and makes the masks of the last.  Its inside and outside
+    charts, both mask sets and the last level's charts and trees equal the
+    independent CKY's."""
+    coarse, fine = split_levels("viterbi", "medium")
+    sents = split_sentences(4, seed=44, n_words=500, mean=8, hi=11)
+    r = oracle.run([coarse, fine, fine], sents, mode="parse")
+    bits = lambda a: a.view(np.int32)
+    c1_in, c1_out, m0, m1 = r.chart(1, "inside"), r.chart(1, "outside"), r.masks(0)[0], r.masks(1)[0]
+    c2_in = r.chart(2, "inside")
+    blocks = node_blocks(r.trees(), [len(x) for x in sents])
+    skipped = 0
+    for s, words in enumerate(sents):
+        n = len(words)
+        ib, it = _viterbi_cky(coarse, words)
+        ob, ot = _viterbi_outside(coarse, words, ib, it)
+        mb0, mt0 = _masks(coarse, words, ib, it, ob, ot)
+        fb1, ft1 = _inside(fine, words, VIT, mb0, mt0, merged=True)
+        ob1, ot1 = _outside(fine, words, fb1, ft1, VIT, mb0, mt0, merged=True)
+        mb1, mt1 = _masks(fine, words, fb1, ft1, ob1, ot1)
+        fb2, ft2 = _inside(fine, words, VIT, mb1, mt1)
+        for b, e, rb, rt in _cells(r, s, n):
+            where = (s, b, e)
+            assert np.array_equal(m0[rb], mb0[b, e]) and np.array_equal(m0[rt], mt0[b, e]), where
+            assert np.array_equal(bits(c1_in[rb]), bits(fb1[b, e])) and np.array_equal(bits(c1_in[rt]), bits(ft1[b, e])), where
+            assert np.array_equal(bits(c1_out[rb]), bits(ob1[b, e])) and np.array_equal(bits(c1_out[rt]), bits(ot1[b, e])), where
+            assert np.array_equal(m1[rb], mb1[b, e]) and np.array_equal(m1[rt], mt1[b, e]), where
+            assert np.array_equal(bits(c2_in[rb]), bits(fb2[b, e])) and np.array_equal(bits(c2_in[rt]), bits(ft2[b, e])), where
+            skipped += int(np.any(mb0[b, e]) and not np.any(fine.jobs["in_NN"]["seg_bits"][0] & mb0[b, e]))
+        if np.isfinite(ft2[0, n, fine.root]):
+            _check_tree(fine, words, fb2, ft2, blocks[s])
+    # some live cells miss segment 0's bits: the merged gate is exercised
+    assert skipped > 0
