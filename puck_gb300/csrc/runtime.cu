@@ -580,7 +580,21 @@ bool build_flat_tiles(LevelDev& D, puck::DevJob& J, int ntgt, int64_t npk, const
 // job's target-major table, grouped by (group of a, group of b), then by
 // segment and target.  Returns false, uploading nothing, when the level's
 // coarse maps do not rise strictly.
-bool group_tiles_host(FlatHost& F, const HostLevel& L, int j, int nseg) {
+// A job's segment bits as its per-pair gates see them.  On a merged level (a
+// middle level of a cascade, the only merged level that receives masks) the
+// reference runs every rule as one block gated by segment 0's bits
+// (CLParser.scala:783-785), so every segment takes segment 0's row and a
+// pair's gate becomes that row: all of the level's pairs pass or none do.
+std::vector<int> gate_seg_bits(const HostLevel& L, const std::string& n, bool merged) {
+  int64_t c = 0;
+  const int* sb = L.get<int>(n + "/seg_bits", "i4", &c);
+  std::vector<int> out(sb, sb + c);
+  if (merged)
+    for (int64_t k = L.mask_size; k < c; ++k) out[k] = sb[k % L.mask_size];
+  return out;
+}
+
+bool group_tiles_host(FlatHost& F, const HostLevel& L, int j, int nseg, bool merged) {
   static const bool a_t[4] = {false, false, true, true};
   static const bool b_t[4] = {false, true, false, true};
   const std::string n = kJobNames[j];
@@ -650,14 +664,15 @@ bool group_tiles_host(FlatHost& F, const HostLevel& L, int j, int nseg) {
   }
   pbk.push_back((int)bs.size());
   bp.push_back((int)rs.size());
+  const std::vector<int> gbits = gate_seg_bits(L, n, merged);
   return flat_tiles_host(F, ntgt, (int64_t)pk.size(), pk.data(), pbk.data(), bs.data(), bp.data(), pr.data(),
-                         pw.data(), L.get<int>(n + "/seg_bits", "i4", nullptr), nseg, L.mask_size, ao.data(),
-                         am.data(), bo.data(), bm.data(), -INFINITY);
+                         pw.data(), gbits.data(), nseg, L.mask_size, ao.data(), am.data(), bo.data(), bm.data(),
+                         -INFINITY);
 }
 
 bool build_group_tiles(LevelDev& D, puck::DevJob& J, const HostLevel& L, int j, int* mtile) {
   FlatHost F;
-  if (!group_tiles_host(F, L, j, J.nseg)) return false;
+  if (!group_tiles_host(F, L, j, J.nseg, D.d.gate_merged != 0)) return false;
   upload_flat(D, J, F, L.mask_size, -INFINITY, mtile);
   return true;
 }
@@ -948,12 +963,19 @@ void puck_host::build_level(LevelDev& D, const HostLevel& L, bool merged) {
     J.a_is_t = a_t[j];
     J.b_is_t = b_t[j];
     J.pair_key = up<int>(D, L, n + "/pair_key", "i4");
-    J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
+    const std::vector<int> gbits = gate_seg_bits(L, n, merged);
+    if (merged && J.nseg > 0) {
+      std::vector<int> g((size_t)npk * L.mask_size);
+      for (size_t k = 0; k < g.size(); ++k) g[k] = gbits[k % L.mask_size];
+      J.pair_gate = static_cast<const int*>(D.upload(g.data(), g.size() * sizeof(int)));
+    } else {
+      J.pair_gate = up<int>(D, L, n + "/pair_gate", "i4");
+    }
     // Viterbi and sum-product jobs (inside and outside) also get the
     // flat-tile layout where it applies
     if ((L.semiring == puck::SEMI_VITERBI || L.semiring == puck::SEMI_REAL) &&
         build_flat_tiles(D, J, ntgt_j, npk, pk, pbk, L.get<int>(n + "/blk_seg", "i4", nullptr), bp, pr, pw,
-                         L.get<int>(n + "/seg_bits", "i4", nullptr), J.nseg, L.mask_size,
+                         gbits.data(), J.nseg, L.mask_size,
                          L.get<int>(a_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
                          L.get<int>(a_t[j] ? "t_mem" : "nt_mem", "i4", nullptr),
                          L.get<int>(b_t[j] ? "t_mem_off" : "nt_mem_off", "i4", nullptr),
@@ -2086,7 +2108,7 @@ int32_t puck_debug_flat_check(const puck_grammar* g, int32_t level, int32_t job,
     FlatHost F;
     bool ok;
     if (form == 1) {
-      ok = group_tiles_host(F, L, job, (int)nseg);
+      ok = group_tiles_host(F, L, job, (int)nseg, false);
     } else {
       int64_t npk = 0;
       const int* pk = L.get<int>(n + "/pair_key", "i4", &npk);
