@@ -80,23 +80,35 @@ def parse_stream(server: CLServer, src: TextIO, sink: TextIO, max_length: int, w
     return n
 
 
-def main(argv: Optional[List[str]] = None) -> int:
+def parse_args(argv: Optional[List[str]] = None) -> argparse.Namespace:
+    """RunParser.Params (RunParser.scala:34-43), same names and defaults."""
     ap = argparse.ArgumentParser(prog="run_parser", description=__doc__.split("\n")[0])
     ap.add_argument("files", nargs="*")
     ap.add_argument("--grammar", default="grammar.grz")
     ap.add_argument("--maxLength", type=int, default=50)
     ap.add_argument("--mem", type=parse_mem, default=parse_mem("3g"))
     ap.add_argument("--profile", type=_bool, nargs="?", const=True, default=False)
-    ap.add_argument("--device", default="0")
+    ap.add_argument("--device", default="nvidia")
     ap.add_argument("--sentences", default="trained")
     ap.add_argument("--tokens", default="default")
     ap.add_argument("--outputSuffix", default=".parsed")
+    # declared by the reference's Params but read by neither RunParser.main
+    # nor anything it calls: accepted so that its command lines run here
+    ap.add_argument("--numToParse", type=int, default=1000)
+    ap.add_argument("--maxParseLength", type=int, default=10000)
     a = ap.parse_args(argv)
     try:
-        segment = preprocess.sentence_segmenter(a.sentences)
-        tokenize = preprocess.tokenizer(a.tokens)
+        preprocess.sentence_segmenter(a.sentences)
+        preprocess.tokenizer(a.tokens)
     except ValueError as exc:
         ap.error(str(exc))
+    return a
+
+
+def main(argv: Optional[List[str]] = None) -> int:
+    a = parse_args(argv)
+    segment = preprocess.sentence_segmenter(a.sentences)
+    tokenize = preprocess.tokenizer(a.tokens)
     device = int(a.device) if a.device.isdigit() else 0
     # sentences with maxLength tokens or more never reach the parser
     server = CLServer(a.grammar, max_alloc_size=a.mem, device=device, max_length=min(max(a.maxLength - 1, 1), 256),

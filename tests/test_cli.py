@@ -178,3 +178,18 @@ def test_treebank_tokens_of_running_text_are_in_the_wsj_vocabulary():
     toks = [t for s in sents for t in treebank_tokens(s)]
     assert [t for t in toks if t not in vocab] == []
     assert sum(t not in vocab for s in sents for t in s.split()) >= 10
+
+
+def test_run_parser_takes_the_reference_params():
+    """Every RunParser.Params field (RunParser.scala:34-43) parses, with the
+    reference's defaults; numToParse and maxParseLength are accepted and, as
+    in the reference's main, unused."""
+    a = run_parser.parse_args([])
+    assert (a.device, a.sentences, a.tokens, a.profile, a.numToParse, a.grammar, a.maxParseLength, a.mem,
+            a.maxLength, a.outputSuffix) == ("nvidia", "trained", "default", False, 1000, "grammar.grz", 10000,
+                                             3 << 30, 50, ".parsed")
+    a = run_parser.parse_args(["--device", "1", "--sentences", "newline", "--tokens", "whitespace", "--profile",
+                               "true", "--numToParse", "5", "--grammar", "g.grz", "--maxParseLength", "40",
+                               "--mem", "2g", "--maxLength", "30", "--outputSuffix", ".out", "a.txt", "b.txt"])
+    assert a.files == ["a.txt", "b.txt"] and a.device == "1" and a.profile is True and a.mem == 2 << 30
+    assert a.maxLength == 30 and a.outputSuffix == ".out" and a.numToParse == 5
