@@ -120,7 +120,8 @@ int32_t puck_grammar_word_id_at(const puck_grammar* g, const char* word, int32_t
 typedef struct puck_compile_options {
   int32_t viterbi;    /* --viterbi (default 1): the fine level's semiring is Viterbi */
   int32_t logsum;     /* --logsum: with viterbi = 0, LogSum instead of Real (CompileGrammar.scala:45-51) */
-  int32_t reproject;  /* --reproject: not supported (PUCK_ERR_INVALID_ARG) */
+  int32_t reproject;  /* --reproject: keep the first and last levels, the last projected onto the
+                         first's substates through its .hierarchy file (CLParser.scala:1153-1209) */
   float threshold;    /* rules and lexicon entries with a lower log score are dropped (-12, as
                          CompileGrammar.scala:56 passes to parseBerkeleyText) */
 } puck_compile_options;

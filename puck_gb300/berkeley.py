@@ -29,6 +29,14 @@ A cascade (``a:b``) shares one coarse label set (the union of the levels'
 numstates labels, first level first) and one vocabulary (the union of the
 levels' lexicon words, sorted), so that masks and word ids mean the same at
 every level.
+
+``reproject`` (CompileGrammar ``--reproject``; CLParser.reprojectGrammar and
+readHierarchy, CLParser.scala:1153-1209) keeps the first and the last level
+and makes the first level's substates the coarse label set: the first level
+projects onto itself, and each substate of the last level onto its ancestor
+at the first level's split depth, read from the last level's ``.hierarchy``
+file.  The two levels' depths are the last run of digits in their prefixes
+(``wsj_1.gr`` is depth 1).
 """
 from __future__ import annotations
 
@@ -89,8 +97,91 @@ class _Reader:
         return prob > 0.0 and math.log(prob) >= self.threshold
 
 
-def read_cascade(prefixes: Sequence[str], threshold: float = -12.0) -> List[Grammar]:
-    """One Grammar per prefix, coarse level first."""
+# -- split hierarchies (readHierarchy) ---------------------------------------
+
+class _Node:
+    __slots__ = ("label", "kids", "start", "end")
+
+    def __init__(self, label: str):
+        self.label, self.kids, self.start, self.end = label, [], 0, 0
+
+    def left_height(self) -> int:
+        return 0 if not self.kids else 1 + self.kids[0].left_height()
+
+    def preorder(self):
+        yield self
+        for k in self.kids:
+            yield from k.preorder()
+
+
+def _parse_bracketed(text: str):
+    """A bracketed split tree: ``(label child ...)``, a child being a subtree
+    or a bare leaf token.  Returns the root and the leaf tokens in order; a
+    node's [start, end) covers its leaves."""
+    toks = re.findall(r"\(|\)|[^\s()]+", text)
+    leaves: List[str] = []
+    pos = 0
+
+    def node() -> _Node:
+        nonlocal pos
+        if toks[pos] != "(":
+            raise ValueError("hierarchy: expected '('")
+        n = _Node(toks[pos + 1])
+        pos += 2
+        n.start = len(leaves)
+        while toks[pos] != ")":
+            if toks[pos] == "(":
+                n.kids.append(node())
+            else:
+                leaves.append(toks[pos])
+                pos += 1
+        pos += 1
+        n.end = len(leaves)
+        return n
+
+    root = node()
+    if pos != len(toks):
+        raise ValueError("hierarchy: trailing tokens")
+    return root, leaves
+
+
+def _depth(prefix: str) -> int:
+    """The split depth of a grammar: the last run of digits in its name."""
+    m = re.match(r"^.*(?:^|[^0-9])([0-9]+)([^0-9]*)$", prefix)
+    if not m:
+        raise ValueError(f"no split depth in {prefix!r}")
+    return int(m.group(1))
+
+
+def read_hierarchy(fine_prefix: str, coarse_prefix: str) -> Dict[str, List[str]]:
+    """Coarse substate -> the fine substates below it, from
+    ``<fine_prefix>.hierarchy`` (one ``SYM (tree)`` line per label)."""
+    fine, coarse = _depth(fine_prefix), _depth(coarse_prefix)
+    out: Dict[str, List[str]] = {}
+    with open(fine_prefix + ".hierarchy", encoding="utf-8") as f:
+        for line in f:
+            parts = line.strip().split(None, 1)
+            if len(parts) != 2:
+                continue
+            sym, (root, leaves) = parts[0], _parse_bracketed(parts[1])
+            total = root.left_height()
+            for sub in root.preorder():
+                if sub.left_height() != total - coarse:
+                    continue
+                if fine - 1 == total:
+                    fines = [f"{sym}_{leaves[i]}" for i in range(sub.start, sub.end)]
+                else:
+                    fines = [f"{sym}_{n.label}" for n in sub.preorder() if n.left_height() == total - fine]
+                out[f"{sym}_{sub.label}"] = fines
+    return out
+
+
+def read_cascade(prefixes: Sequence[str], threshold: float = -12.0, reproject: bool = False) -> List[Grammar]:
+    """One Grammar per prefix, coarse level first.  With ``reproject`` and
+    more than one prefix: the first and last levels, projected onto the
+    first level's substates."""
+    if reproject and len(prefixes) > 1:
+        return _reprojected(prefixes[0], prefixes[-1], threshold)
     readers = [_Reader(p, threshold) for p in prefixes]
     coarse_names: List[str] = []
     seen = set()
@@ -102,11 +193,44 @@ def read_cascade(prefixes: Sequence[str], threshold: float = -12.0) -> List[Gram
     coarse_id = {n: i for i, n in enumerate(coarse_names)}
     vocab = sorted({w for r in readers for _, w, _ in r.lexicon})
     word_id = {w: i for i, w in enumerate(vocab)}
-    return [_grammar(r, coarse_names, coarse_id, vocab, word_id) for r in readers]
+
+    def by_base(r):
+        def project(name: str) -> int:
+            base, _ = _split_label(name)
+            if base not in coarse_id:
+                raise ValueError(f"{r.prefix}: label {name!r} has no numstates entry")
+            return coarse_id[base]
+        return project
+
+    return [_grammar(r, coarse_names, by_base(r), vocab, word_id) for r in readers]
 
 
-def _grammar(r: _Reader, coarse_names: List[str], coarse_id: Dict[str, int], vocab: List[str],
+def _reprojected(coarse_prefix: str, fine_prefix: str, threshold: float) -> List[Grammar]:
+    rc, rf = _Reader(coarse_prefix, threshold), _Reader(fine_prefix, threshold)
+    coarse_names = [f"{name}_{i}" for name, k in rc.numstates for i in range(k)]
+    coarse_id = {n: i for i, n in enumerate(coarse_names)}
+    up = {f: c for c, fs in read_hierarchy(fine_prefix, coarse_prefix).items() for f in fs}
+    vocab = sorted({w for r in (rc, rf) for _, w, _ in r.lexicon})
+    word_id = {w: i for i, w in enumerate(vocab)}
+
+    def itself(name: str) -> int:
+        if name not in coarse_id:
+            raise ValueError(f"{coarse_prefix}: label {name!r} has no numstates entry")
+        return coarse_id[name]
+
+    def through_hierarchy(name: str) -> int:
+        c = name if name == "ROOT_0" else up.get(name)   # the root projects onto itself
+        if c is None or c not in coarse_id:
+            raise ValueError(f"{fine_prefix}: substate {name!r} has no ancestor among {coarse_prefix}'s")
+        return coarse_id[c]
+
+    return [_grammar(rc, coarse_names, itself, vocab, word_id),
+            _grammar(rf, coarse_names, through_hierarchy, vocab, word_id)]
+
+
+def _grammar(r: _Reader, coarse_names: List[str], project, vocab: List[str],
              word_id: Dict[str, int]) -> Grammar:
+    """``project(substate name) -> coarse id``."""
     labels: List[str] = []
     coarse: List[int] = []
     lid: Dict[str, int] = {}
@@ -114,16 +238,14 @@ def _grammar(r: _Reader, coarse_names: List[str], coarse_id: Dict[str, int], voc
         for i in range(k):
             lid[f"{name}_{i}"] = len(labels)
             labels.append(f"{name}_{i}")
-            coarse.append(coarse_id[name])
+            coarse.append(project(f"{name}_{i}"))
 
     def label(name: str) -> int:
         if name not in lid:
-            base, _ = _split_label(name)
-            if base not in coarse_id:
-                raise ValueError(f"{r.prefix}: label {name!r} has no numstates entry")
+            _split_label(name)
             lid[name] = len(labels)
             labels.append(name)
-            coarse.append(coarse_id[base])
+            coarse.append(project(name))
         return lid[name]
 
     bins = [(label(p), label(a), label(b), math.log(pr)) for p, a, b, pr in r.binary if r.keep(pr)]

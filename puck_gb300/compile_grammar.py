@@ -5,8 +5,9 @@ Same flags and meaning: ``--textGrammarPrefix a:b`` (Berkeley text grammars,
 coarse first), ``--grammar out.grz``, ``--viterbi`` (default true; the fine
 level's semiring), ``--logsum`` (used when ``--viterbi false``; otherwise the
 Real semiring).  Coarse levels are always Viterbi.  ``--device`` is accepted
-and ignored (the tables are built on the host).  ``--reproject`` is refused:
-it needs epic's projection machinery.
+and ignored (the tables are built on the host).  ``--reproject`` keeps the
+first and last levels and projects the last onto the first's substates
+through the last level's ``.hierarchy`` file (berkeley.read_cascade).
 
 Extra flag for the synthetic workloads: ``--synthetic split|pcfg`` with
 ``--seed`` builds the seeded split-grammar cascade or the plain PCFG instead
@@ -49,8 +50,8 @@ def main(argv: Optional[List[str]] = None) -> int:
     ap.add_argument("--seed", type=int, default=1)
     a = ap.parse_args(argv)
     sem = fine_semiring(a.viterbi, a.logsum)
-    if a.reproject:
-        print("compile_grammar: --reproject is not supported", file=sys.stderr)
+    if a.reproject and a.synthetic:
+        print("compile_grammar: --reproject needs --textGrammarPrefix", file=sys.stderr)
         return 2
     if a.synthetic == "split":
         c, f = synth.split_grammar(seed=a.seed)
@@ -58,7 +59,7 @@ def main(argv: Optional[List[str]] = None) -> int:
     elif a.synthetic == "pcfg":
         grammars = [synth.small_pcfg(a.seed)]
     elif a.textGrammarPrefix:
-        grammars = berkeley.read_cascade(a.textGrammarPrefix.split(":"), a.threshold)
+        grammars = berkeley.read_cascade(a.textGrammarPrefix.split(":"), a.threshold, reproject=a.reproject)
     else:
         ap.error("give --textGrammarPrefix or --synthetic")
     levels = [grammar.compile_level(g, "viterbi") for g in grammars[:-1]]

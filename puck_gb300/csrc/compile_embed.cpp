@@ -133,10 +133,6 @@ extern "C" puck_status puck_compile_grammar(const char* text_prefixes, const cha
   puck_compile_options o;
   puck_default_compile_options(&o);
   if (opts) o = *opts;
-  if (o.reproject) {
-    puck::set_last_error("puck_compile_grammar: reproject is not supported (it needs epic's projections)");
-    return PUCK_ERR_INVALID_ARG;
-  }
   std::lock_guard<std::mutex> lk(g_py_mu);
   std::string why;
   if (!python(&why)) {
@@ -154,7 +150,8 @@ extern "C" puck_status puck_compile_grammar(const char* text_prefixes, const cha
       "    from puck_gb300 import compile_grammar as _cg\n"
       "    rc = _cg.main(['--textGrammarPrefix', " + py_str(text_prefixes) + ", '--grammar', " +
       py_str(out_grz) + ", '--viterbi', '" + (o.viterbi ? "true" : "false") + "', '--logsum', '" +
-      (o.logsum ? "true" : "false") + "', '--threshold', '" + thr + "'])\n"
+      (o.logsum ? "true" : "false") + "', '--reproject', '" + (o.reproject ? "true" : "false") +
+      "', '--threshold', '" + thr + "'])\n"
       "    err = '' if rc == 0 else 'compile_grammar exited with status %d' % rc\n"
       "except SystemExit as e:\n"
       "    rc, err = 2, 'compile_grammar: bad arguments (%s)' % e\n"

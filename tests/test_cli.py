@@ -44,9 +44,68 @@ def test_compile_grammar_synthetic_writes_a_loadable_archive(tmp_path):
     assert len(levels) == 1 and not levels[0].is_viterbi
 
 
-def test_compile_grammar_refuses_reproject(tmp_path):
+def _hierarchy_pair(tmp_path):
+    """tg_1 (2 substates per label) and tg_2 (4), with tg_2's hierarchy
+    putting substates 0 and 2 under tg_1's 0, and 1 and 3 under its 1."""
+    from helpers import write_text_grammar
+    c = write_text_grammar(str(tmp_path), "tg_1", 2, seed=5)
+    f = write_text_grammar(str(tmp_path), "tg_2", 4, seed=6)
+    with open(f + ".hierarchy", "w") as h:
+        for lab in ("S", "NP", "VP", "DT", "NN", "VB"):
+            h.write(f"{lab}\t(0 (0 (0 0) (2 2)) (1 (1 1) (3 3)))\n")
+    return c, f
+
+
+def test_reproject_maps_fine_substates_through_the_hierarchy(tmp_path):
+    c, f = _hierarchy_pair(tmp_path)
+    assert berkeley.read_hierarchy(f, c)["NP_0"] == ["NP_0", "NP_2"]
+    gc, gf = berkeley.read_cascade([c, f], reproject=True)
+    names = gc.coarse_names
+    assert names == gc.labels                        # the coarse level projects onto itself
+    assert [names[gc.coarse[i]] for i in range(len(gc.labels))] == gc.labels
+    proj = {gf.labels[i]: names[gf.coarse[i]] for i in range(len(gf.labels))}
+    assert proj["VP_2"] == "VP_0" and proj["VP_3"] == "VP_1" and proj["ROOT_0"] == "ROOT_0"
+    levels = [grammar.compile_level(gc), grammar.compile_level(gf)]
+    wid = {w: i for i, w in enumerate(gf.words)}
+    sent = np.array([wid[w] for w in "the dog sees a cat".split()], np.int32)
+    r = oracle.run(levels, [sent], mode="parse")
+    assert np.isfinite(r.trees()[0, 3:4].view(np.float32)[0])
+    # the command line: a written archive; --reproject with --synthetic is refused
+    out = str(tmp_path / "r.grz")
+    assert compile_grammar.main(["--textGrammarPrefix", f"{c}:{f}", "--grammar", out, "--reproject"]) == 0
+    assert [lv.n_coarse for lv in grz.read_sequence(out)] == [len(gc.labels)] * 2
     assert compile_grammar.main(["--synthetic", "pcfg", "--grammar", str(tmp_path / "g.grz"),
                                  "--reproject"]) == 2
+
+
+def test_read_hierarchy_leaf_level(tmp_path):
+    """A fine level one below the tree's height takes the tree's leaves."""
+    p = str(tmp_path / "h_3")
+    for name in ("h_3", "h_2"):
+        with open(str(tmp_path / name) + ".hierarchy", "w") as h:
+            h.write("X\t(0 (0 (0 0 1) (1 2)) (1 (2 3 4)))\n")
+    assert berkeley.read_hierarchy(p, str(tmp_path / "h_1")) == {"X_0": ["X_0", "X_1", "X_2"], "X_1": ["X_3", "X_4"]}
+    assert berkeley.read_hierarchy(str(tmp_path / "h_2"), str(tmp_path / "h_0")) == {
+        "X_0": ["X_0", "X_1", "X_2"]}
+
+
+@pytest.mark.skipif(not os.path.exists(TEXT + "/wsj_1.gr.binary"), reason="reference text grammars absent")
+def test_reproject_of_wsj_0_1_equals_the_base_label_projection():
+    """wsj_0 has one substate per label, so projecting wsj_1 onto wsj_0's
+    substates through the hierarchy is the base-label projection renamed:
+    same masks and trees."""
+    plain = berkeley.read_cascade([TEXT + "/wsj_0.gr", TEXT + "/wsj_1.gr"])
+    rep = berkeley.read_cascade([TEXT + "/wsj_0.gr", TEXT + "/wsj_1.gr"], reproject=True)
+    base = lambda n: n.rsplit("_", 1)[0]
+    for a, b in zip(plain, rep):
+        assert a.labels == b.labels
+        assert [a.coarse_names[x] for x in a.coarse] == [base(b.coarse_names[x]) for x in b.coarse]
+    wid = {w: i for i, w in enumerate(plain[1].words)}
+    sents = [np.array([wid[w] for w in s.split()], np.int32)
+             for s in ("The company said it expects revenue to rise .", "He sold shares of the stock .")]
+    runs = [oracle.run([grammar.compile_level(g, "viterbi") for g in gs], sents, mode="parse") for gs in (plain, rep)]
+    assert np.array_equal(runs[0].trees(), runs[1].trees())
+    assert np.array_equal(runs[0].masks(0)[0], runs[1].masks(0)[0])
 
 
 class _FakeServer:

@@ -180,8 +180,14 @@ def test_compile_grammar_through_the_c_abi_matches_the_python_compiler(tmp_path)
     L = _lib.load()
     opts = (ctypes.c_int32 * 4)()
     L.puck_default_compile_options(ctypes.byref(opts))
+    # reproject through the C ABI equals the command line's --reproject
+    from test_cli import _hierarchy_pair
+    hc, hf = _hierarchy_pair(tmp_path)
     opts[2] = 1  # reproject
-    assert L.puck_compile_grammar(f"{c}:{f}".encode(), str(tmp_path / "r.grz").encode(), ctypes.byref(opts)) == 6
+    abi, py = str(tmp_path / "r_abi.grz"), str(tmp_path / "r_py.grz")
+    assert L.puck_compile_grammar(f"{hc}:{hf}".encode(), abi.encode(), ctypes.byref(opts)) == 0, _lib.last_error()
+    assert compile_grammar.main(["--textGrammarPrefix", f"{hc}:{hf}", "--grammar", py, "--reproject"]) == 0
+    _same_archives(abi, py)
 
 
 def test_compile_grammar_from_a_host_without_python(tmp_path):
