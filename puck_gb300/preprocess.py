@@ -85,18 +85,26 @@ def newline_sentences(src: TextIO) -> Iterator[str]:
 
 
 def rule_sentences(src: TextIO) -> Iterator[str]:
-    """Running text, paragraph by paragraph (blank-line separated), each
-    paragraph split by :func:`segment` as soon as it is complete."""
-    para: List[str] = []
+    """Running text split by :func:`segment`, streamed: a boundary depends
+    only on the words around it, so every sentence but the last of the text
+    read so far is final and is yielded at once; the unfinished rest waits
+    for more lines.  A blank line ends a paragraph, and no sentence crosses
+    it."""
+    buf = ""
     for line in src:
-        if line.strip():
-            para.append(line)
+        text = line.strip()
+        if not text:
+            if buf:
+                yield from segment(buf)
+            buf = ""
             continue
-        if para:
-            yield from segment(" ".join(para))
-            para = []
-    if para:
-        yield from segment(" ".join(para))
+        buf = f"{buf} {text}" if buf else text
+        parts = segment(buf)
+        if len(parts) > 1:
+            yield from parts[:-1]
+            buf = parts[-1]
+    if buf:
+        yield from segment(buf)
 
 
 # -- tokens ------------------------------------------------------------------

@@ -58,6 +58,28 @@ def test_rule_sentences_do_not_cross_blank_lines():
                                                     "third paragraph without a stop"]
 
 
+def test_rule_sentences_stream():
+    """A sentence is yielded as soon as the line after its end has been
+    read, not at the end of the input."""
+    read = []
+
+    def lines():
+        for i, line in enumerate(["One sentence here. Another one", "starts here. And a", "third.", ""]):
+            read.append(i)
+            yield line + "\n"
+
+    it = preprocess.rule_sentences(lines())
+    assert next(it) == "One sentence here." and read == [0]
+    assert next(it) == "Another one starts here." and read == [0, 1]
+    assert list(it) == ["And a third."]
+    # the streamed split equals splitting the whole paragraph at once
+    text = ("Mr. Smith went to Washington. He met J. Doe at the U.S. Capitol. "
+            '"Is it done?" she asked. Yes! The end... Prices rose 5. Then they fell.')
+    words = text.split()
+    chunks = [" ".join(words[i:i + 3]) + "\n" for i in range(0, len(words), 3)]
+    assert list(preprocess.rule_sentences(io.StringIO("".join(chunks)))) == segment(text)
+
+
 def test_flag_values_follow_the_reference():
     assert preprocess.sentence_segmenter("newline") is preprocess.newline_sentences
     for v in ("java", "trained", "default", "TRAINED"):
