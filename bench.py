@@ -153,6 +153,22 @@ def cpu_baseline(levels, sents, sample: int):
                       f"fine inside, backtrace; {dt:.1f}s"}, r
 
 
+def e2e_roofline(P, nlevels: int, dev_ms, fp32_peak: float) -> dict:
+    """The end-to-end fraction: every level's binary-pass work of the last
+    timed step (each step parses the same workload) at the FP32 lane peak,
+    over the step's device time.  The HBM-bound kernels (lexicon, masks,
+    decode) are a few percent of device time and are left out."""
+    try:
+        step_ops = 2.0 * sum(P.level_work(l)[0] for l in range(nlevels))
+        step_s = sum(dev_ms) / len(dev_ms) / 1e3
+        return {"frac": round(step_ops / (fp32_peak * 1e12) / step_s, 4), "ops_per_step": step_ops,
+                "peak": round(fp32_peak, 2), "unit": "TFLOP/s",
+                "note": "all levels' binary passes (2 ops per work unit) at the FP32 lane peak / device "
+                        "time per step; HBM-bound kernels not counted"}
+    except Exception as exc:  # a report, never a reason to lose the line
+        return {"unavailable": str(exc)[:160]}
+
+
 def reference_work(r, value: float) -> dict:
     """The reference's work measure on the CPU-baseline sample: (rule, split)
     applications its binary queues run in the last level's inside pass
@@ -428,6 +444,7 @@ def run_ours(args):
         "pruning": {"cells": int(s["cells"]), "cells_pruned": int(s["cells_pruned"]),
                     "fraction": round(s["cells_pruned"] / max(s["cells"], 1), 4)},
     }
+    out["e2e_roofline"] = e2e_roofline(P, len(levels), dev_ms, fp32_peak)
     P.release()
     if rank == 0 and world == 1:
         if args.cpu_sample > 0:

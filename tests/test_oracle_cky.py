@@ -753,3 +753,26 @@ def test_three_level_cascade_with_a_merged_middle_level():
             _check_tree(fine, words, fb2, ft2, blocks[s])
     # some live cells miss segment 0's bits: the merged gate is exercised
     assert skipped > 0
+
+
+def test_bench_e2e_roofline_arithmetic():
+    """bench.py's end-to-end fraction from a parser's per-level work: 2 ops
+    per unit over all levels, at the peak, over the mean device time; a
+    failing parser call gives an 'unavailable' entry instead of an error."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+
+    class FakeParser:
+        def level_work(self, level):
+            return ((1e12, 0), (3e12, 0))[level]
+
+    rep = bench.e2e_roofline(FakeParser(), 2, [2000.0, 2000.0], 40.0)
+    assert rep["ops_per_step"] == 8e12 and rep["frac"] == round(8e12 / 40e12 / 2.0, 4)
+
+    class Broken:
+        def level_work(self, level):
+            raise RuntimeError("no device")
+
+    assert "unavailable" in bench.e2e_roofline(Broken(), 2, [1.0], 40.0)
