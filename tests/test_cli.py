@@ -44,15 +44,19 @@ def test_compile_grammar_synthetic_writes_a_loadable_archive(tmp_path):
     assert len(levels) == 1 and not levels[0].is_viterbi
 
 
-def _hierarchy_pair(tmp_path):
+def _hierarchy_pair(tmp_path, interleaved=True):
     """tg_1 (2 substates per label) and tg_2 (4), with tg_2's hierarchy
-    putting substates 0 and 2 under tg_1's 0, and 1 and 3 under its 1."""
+    putting substates 0 and 2 under tg_1's 0, and 1 and 3 under its 1 (or,
+    not interleaved, 0 and 1 under 0, and 2 and 3 under 1)."""
     from helpers import write_text_grammar
-    c = write_text_grammar(str(tmp_path), "tg_1", 2, seed=5)
-    f = write_text_grammar(str(tmp_path), "tg_2", 4, seed=6)
+    d = tmp_path / ("interleaved" if interleaved else "contiguous")
+    d.mkdir(exist_ok=True)
+    c = write_text_grammar(str(d), "tg_1", 2, seed=5)
+    f = write_text_grammar(str(d), "tg_2", 4, seed=6)
+    tree = "(0 (0 (0 0) (2 2)) (1 (1 1) (3 3)))" if interleaved else "(0 (0 (0 0) (1 1)) (1 (2 2) (3 3)))"
     with open(f + ".hierarchy", "w") as h:
         for lab in ("S", "NP", "VP", "DT", "NN", "VB"):
-            h.write(f"{lab}\t(0 (0 (0 0) (2 2)) (1 (1 1) (3 3)))\n")
+            h.write(f"{lab}\t{tree}\n")
     return c, f
 
 

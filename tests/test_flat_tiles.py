@@ -120,3 +120,32 @@ def test_flat_check_rejects_bad_arguments():
         assert L.puck_debug_flat_check(g, 0, 0, 3, out) == -3   # no such form
     finally:
         L.puck_grammar_free(g)
+
+
+def test_flat_tables_need_contiguous_members(tmp_path):
+    """A reprojected cascade whose hierarchy interleaves the fine substates
+    (0 and 2 under one coarse substate, 1 and 3 under the other) gives
+    coarse symbols whose members are not contiguous in symbol order.  The
+    flat-tile layout, which addresses a tile's members as one index range,
+    is declined for them (the level keeps the whole-pair form, which reads
+    members through the member lists); the same cascade with a contiguous
+    hierarchy gets it for all twelve jobs, every rule held once."""
+    from test_cli import _hierarchy_pair
+    from puck_gb300 import berkeley, grammar
+    for interleaved in (True, False):
+        c, f = _hierarchy_pair(tmp_path, interleaved)
+        gc, gf = berkeley.read_cascade([c, f], reproject=True)
+        members = [[gf.labels[i] for i in range(len(gf.labels)) if gf.coarse[i] == k]
+                   for k in range(len(gc.labels))]
+        assert (["NP_0", "NP_2"] if interleaved else ["NP_0", "NP_1"]) in members
+        levels = (grammar.compile_level(gc), grammar.compile_level(gf))
+        L, g = _grammar(levels, f"reprojected_{'interleaved' if interleaved else 'contiguous'}")
+        try:
+            out = (ctypes.c_int64 * 4)()
+            codes = [L.puck_debug_flat_check(g, 1, job, 0, out) for job in JOBS]
+        finally:
+            L.puck_grammar_free(g)
+        if interleaved:
+            assert codes[0] == -1 and all(rc in (-1, 0) for rc in codes), codes
+        else:
+            assert codes == [0] * len(JOBS), codes
